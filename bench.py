@@ -1,0 +1,505 @@
+"""Benchmark: exact sorted-u32 pair intersection on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one step): the skewed 2-set sweep -- four independent pairs with
+|large| = 2^24 and |small| in {2^10, 2^14, 2^18, 2^24}, element space
+m = |large| / 0.05, selectivity 1% of |small|, seeded synthetic data shaped
+like the reference's generator (benchmark/src/generators.rs:30-68).  Each
+pair is intersected exactly (materialised, ascending) with the algorithm the
+policy picks for its size ratio.
+
+* ``value``: pair intersections/s with inputs resident in HBM (device
+  pointers, async C-ABI calls), timed with CUDA events over K steps.
+* ``e2e``: the same through the host-pointer C-ABI call
+  (``setops_gpu_intersect(..., SETOPS_HOST)``): pinned host inputs copied in
+  and the result copied out inside the timed region.
+* ``roofline``: the merge-path kernel on the 2^24 x 2^24 pair; algorithmic
+  bytes = both inputs read + output written, over its CUDA-event time.
+* ``cpu_baseline``: the reference's CPU path (oracle port: best of
+  shuffling / SIMD galloping / bmiss per pair) on this host's cores.
+
+``--impl reference`` times that CPU path alone on all host threads (pairs
+spread over threads), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "pair intersections/sec & GB/s vs HBM peak (exact)"
+UNIT = "pair-intersections/s"
+SMALL_EXPS = (10, 14, 18, 24)
+LARGE = 1 << 24
+DENSITY = 0.05
+SELECTIVITY = 0.01
+SEED = 20240601
+HEADLINE = 3  # index of the 2^24 x 2^24 pair
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_sweep(rank: int):
+    from simd_set_operations_gb300 import datasets as ds
+    pairs = []
+    for k, e in enumerate(SMALL_EXPS):
+        s, l = ds.gen_twoset(SEED + 1000 * rank + k, DENSITY, SELECTIVITY, 1 << e, LARGE)
+        pairs.append((s, l))
+    return pairs
+
+
+def algorithmic_bytes(ns: int, nl: int, nout: int) -> int:
+    return 4 * (ns + nl) + 4 * nout
+
+
+def workload_config():
+    return {
+        "workload": "skewed 2-set sweep: |large| = 2^24, |small| in {2^10, 2^14, 2^18, 2^24}, "
+                    "density 0.05, selectivity 0.01, materialised sorted output",
+        "pairs_per_step": len(SMALL_EXPS),
+        "small_sizes": [1 << e for e in SMALL_EXPS],
+        "large_size": LARGE,
+        "element_space": int(LARGE / DENSITY),
+        "density": DENSITY,
+        "selectivity": SELECTIVITY,
+        "seed": SEED,
+        "l2": "inputs larger than L2: 321 MiB read per step vs 129 MB L2, each array "
+              "touched once per step; no flush",
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+CLOCK_Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"setops_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={CLOCK_Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU path (oracle port of the reference's CPU algorithms)
+
+def cpu_sweep_best(pairs, nthreads: int, seconds: float):
+    """Times each baseline on each pair (pairs spread over `nthreads`
+    threads), picks the best algorithm per pair, and returns (pairs/s for a
+    full sweep with the best per-pair algorithms, details)."""
+    import oracle
+    algos = [oracle.SHUFFLING_W8, oracle.SIMD_GALLOPING_W16, oracle.BMISS_W4]
+    outs = [np.empty(min(s.size, l.size), np.uint32) for s, l in pairs]
+    best = []
+    t_total = 0.0
+    counts = None
+    for i, (s, l) in enumerate(pairs):
+        times = {}
+        for a in algos:
+            reps, t0 = 0, time.perf_counter()
+            while True:
+                c = oracle.run_pairs(a, [(s, l)], 1, outs=[outs[i]])
+                reps += 1
+                el = time.perf_counter() - t0
+                if el > seconds / (len(pairs) * len(algos)) or reps >= 50:
+                    break
+            times[a] = el / reps
+            t_total += el
+        a = min(times, key=times.get)
+        best.append((a, times[a], times))
+    # full sweep with best algorithm per pair, pairs spread over threads
+    groups = {}
+    for i, (a, _, _) in enumerate(best):
+        groups.setdefault(a, []).append(i)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        if nthreads > 1:
+            import threading
+            res = {}
+
+            def run(a, idx):
+                res[a] = oracle.run_pairs(a, [pairs[i] for i in idx], len(idx))
+            ths = [threading.Thread(target=run, args=(a, idx)) for a, idx in groups.items()]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+        else:
+            res = {a: oracle.run_pairs(a, [pairs[i] for i in idx], 1) for a, idx in groups.items()}
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > max(1.0, seconds / 4) or reps >= 20:
+            break
+    counts = [0] * len(pairs)
+    for a, idx in groups.items():
+        for j, i in enumerate(idx):
+            counts[i] = int(res[a][j])
+    sweep_s = el / reps
+    detail = [{"small": int(s.size), "large": int(l.size),
+               "best": oracle.ALGO_NAMES[a], "seconds": t,
+               "all": {oracle.ALGO_NAMES[k]: v for k, v in tt.items()}}
+              for (s, l), (a, t, tt) in zip(pairs, best)]
+    return len(pairs) / sweep_s, sweep_s, detail, counts, outs, t_total + el
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.lib()
+    cores = oracle.host_cores()
+    pairs = make_sweep(0)
+    # warmup: algorithm choice per pair (bounded)
+    _, _, detail, _, _, _ = cpu_sweep_best(pairs, 1, min(args.cpu_sample_seconds, 6.0))
+    best = [next(k for k, v in oracle.ALGO_NAMES.items() if v == d["best"]) for d in detail]
+    groups = {}
+    for i, a in enumerate(best):
+        groups.setdefault(a, []).append(i)
+    import threading
+
+    def sweep():
+        res = {}
+
+        def run(a, idx):
+            res[a] = oracle.run_pairs(a, [pairs[i] for i in idx], max(1, min(len(idx), cores)))
+        ths = [threading.Thread(target=run, args=(a, idx)) for a, idx in groups.items()]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        return res
+
+    for _ in range(max(args.warmup, 1)):
+        sweep()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sweep()
+    el = time.perf_counter() - t0
+    value = len(pairs) * args.steps / el
+    used = min(cores, len(pairs))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": f"{args.steps} full sweeps (4 pairs each), best algorithm per "
+                                   "pair, pairs spread over threads",
+                         "algorithms": detail, "host_cores": cores,
+                         "arch": os.uname().machine},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+def read_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def read_traffic():
+    """DRAM bytes per launch of the headline kernel from the committed ncu
+    summary (profiles/), or None."""
+    f = ROOT / "profiles" / "merge_2e24x2e24_ncu.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read_text())
+    return int(m.group(1)) if m else None
+
+
+def run_gb300(args):
+    import ctypes as C
+
+    import torch
+
+    import simd_set_operations_gb300 as so
+    from simd_set_operations_gb300 import _lib
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    ctx = so.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    L = _lib.lib
+
+    pairs = make_sweep(rank)
+    dev = []
+    for s, l in pairs:
+        ds_ = torch.from_numpy(s.view(np.int32)).cuda()
+        dl_ = torch.from_numpy(l.view(np.int32)).cuda()
+        out = torch.empty(s.size, dtype=torch.int32, device="cuda")
+        dev.append((ds_, dl_, out))
+    lens = torch.zeros(len(pairs), dtype=torch.int64, device="cuda")
+    h = ctx.handle
+
+    def step(ev=None):
+        for i, ((s, l), (ds_, dl_, out)) in enumerate(zip(pairs, dev)):
+            if ev is not None:
+                ev[i][0].record(stream)
+            rc = L.setops_gpu_intersect_async(h, ds_.data_ptr(), s.size, dl_.data_ptr(), l.size,
+                                              out.data_ptr(), s.size,
+                                              lens.data_ptr() + 8 * i, 0)
+            if rc != 0:
+                ctx.check(rc)
+            if ev is not None:
+                ev[i][1].record(stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warmup (at least W steps and about 2 s of load for the clock sampler)
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_w = time.perf_counter()
+    nw = 0
+    while nw < args.warmup or time.perf_counter() - t_w < 2.0:
+        step()
+        nw += 1
+        if nw % 50 == 0:
+            torch.cuda.synchronize()
+    torch.cuda.synchronize()
+    ctx.synchronize()
+
+    # exactness of the step's results (counts are known from generation)
+    got = lens.cpu().tolist()
+    want = [int(SELECTIVITY * s.size) for s, _ in pairs]
+    if got != want:
+        raise SystemExit(f"wrong intersection sizes {got} != {want}")
+
+    # timed region: K steps, no host synchronisation inside; one event pair
+    # around every launch (on the launching stream) for per-kernel times
+    def mk():
+        return torch.cuda.Event(enable_timing=True)
+    evs = [[(mk(), mk()) for _ in pairs] for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count
+    t_start, t_end = mk(), mk()
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launch_count - launches0
+    clocks = sampler.stop()
+    per_pair = [[evs[k][i][0].elapsed_time(evs[k][i][1]) for k in range(args.steps)]
+                for i in range(len(pairs))]
+    dev_ms = sum(sum(p) for p in per_pair)
+    wall_ms = t_start.elapsed_time(t_end)
+    el_s = wall_ms / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([el_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_s = float(t.item())
+    value = world * len(pairs) * args.steps / el_s
+
+    # roofline: headline merge kernel
+    s_h, l_h = pairs[HEADLINE]
+    nout = int(SELECTIVITY * s_h.size)
+    head_ms = statistics.mean(per_pair[HEADLINE])
+    algo_bytes = algorithmic_bytes(s_h.size, l_h.size, nout)
+    achieved = algo_bytes / (head_ms / 1e3) / 1e9
+    peak, peak_kind = read_peak()
+    traffic = read_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "merge_kernel (2^24 x 2^24 pair, materialise)",
+                "algorithmic_bytes_per_launch": algo_bytes,
+                "launch_ms_mean": head_ms, "peak_source": f"{peak_kind} (hbm_gbs)"}
+    sweep = []
+    for (s, l), p in zip(pairs, per_pair):
+        n = int(SELECTIVITY * s.size)
+        ms = statistics.mean(p)
+        sweep.append({"small": int(s.size), "large": int(l.size), "out": n,
+                      "ms_mean": ms, "ms_min": min(p),
+                      "GBps_algorithmic": algorithmic_bytes(s.size, l.size, n) / (ms / 1e3) / 1e9})
+
+    # e2e through the host-pointer C ABI
+    e2e = None
+    if not args.no_e2e:
+        pinned = []
+        for s, l in pairs:
+            ps = torch.from_numpy(s.view(np.int32)).pin_memory().numpy().view(np.uint32)
+            pl = torch.from_numpy(l.view(np.int32)).pin_memory().numpy().view(np.uint32)
+            po = torch.empty(s.size, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+            pinned.append((ps, pl, po))
+        ctx.set_stream(None)
+        n_out = C.c_size_t()
+
+        def step_e2e():
+            tot_out = 0
+            for ps, pl, po in pinned:
+                rc = L.setops_gpu_intersect(h, ps.ctypes.data, ps.size, pl.ctypes.data, pl.size,
+                                            po.ctypes.data, ps.size, C.byref(n_out), _lib.HOST)
+                if rc != 0:
+                    ctx.check(rc)
+                tot_out += n_out.value
+            return tot_out
+
+        for _ in range(max(2, args.warmup // 2)):
+            step_e2e()
+        e2e_steps = max(3, min(args.steps, 20))
+        barrier()
+        t0 = time.perf_counter()
+        tot_out = 0
+        for _ in range(e2e_steps):
+            tot_out = step_e2e()
+        e_el = time.perf_counter() - t0
+        barrier()
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e_el], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_el = float(t.item())
+        h2d = sum(4 * (s.size + l.size) for s, l in pairs)
+        d2h = 4 * tot_out + 8 * len(pairs)
+        e2e = {"value": world * len(pairs) * e2e_steps / e_el, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+               "ms_per_step": 1e3 * e_el / e2e_steps,
+               "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers"}
+        ctx.set_stream(stream)
+
+    # CPU baseline (rank 0 at N=1 only), also the cross-check of the results
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        cores = oracle.host_cores()
+        v1, s1, detail, counts, outs, spent = cpu_sweep_best(pairs, 1, args.cpu_sample_seconds)
+        vall, sall, _, _, _, spent2 = cpu_sweep_best(pairs, min(cores, len(pairs)), 2.0)
+        for i, ((s, l), (ds_, dl_, out)) in enumerate(zip(pairs, dev)):
+            n = int(lens[i])
+            g = out[:n].cpu().numpy().view(np.uint32)
+            if n != counts[i] or not np.array_equal(g, outs[i][:n]):
+                raise SystemExit(f"GPU result of pair {i} differs from the CPU path")
+        cpu = {"value": vall, "unit": UNIT, "cores": min(cores, len(pairs)), "kind": "port",
+               "sample": "the 4-pair sweep; each baseline timed per pair, best per pair kept; "
+                         "all-cores = pairs spread over threads (one pair never spans threads)",
+               "single_core": {"value": v1, "cores": 1, "sweep_seconds": s1},
+               "algorithms": detail, "cpu_seconds_spent": spent + spent2,
+               "host_cores": cores, "arch": os.uname().machine,
+               "results_match_gpu": True}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded; reference generator shape)",
+        "config": workload_config(),
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep,
+        "timing": {"bracket_ms_total": wall_ms, "kernel_ms_total": dev_ms,
+                   "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
+                           "sync inside); kernel_ms_total sums the per-launch events"},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,89 @@
+/*
+ * setops_bench.h -- benchmark-side helpers exported by libsetops_gpu.so:
+ * seeded synthetic set generators and the reference's on-disk datafile
+ * format.  Host code only; no GPU needed.
+ *
+ * The generators restate benchmark/src/generators.rs of
+ * UNSW-database/simd_set_operations with a seeded PRNG (xoshiro256**, seeded
+ * by SplitMix64) in place of the reference's unseeded thread_rng
+ * (generators.rs:87), so inputs are reproducible; the value distributions and
+ * the shared/unshared construction are the reference's.
+ */
+#ifndef SETOPS_BENCH_H
+#define SETOPS_BENCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* gen_twoset (benchmark/src/generators.rs:30-68) for explicit lengths:
+ * max_value = floor(large_len / density); floor(selectivity * small_len)
+ * shared elements plus disjoint fills, drawn without replacement from
+ * [0, max_value) (shuffled_set, generators.rs:83-110), then sorted.  Returns
+ * 0, or -1 on bad arguments. */
+int setops_gen_twoset(uint64_t seed, double density, double selectivity,
+                      size_t small_len, size_t large_len, uint32_t *small_out,
+                      uint32_t *large_out);
+
+/* Set lengths of gen_kset (generators.rs:112-135, get_skew :220-224):
+ * lens[i] = max_len / floor((i+1)^skewness), listed smallest first (the
+ * reference emits sets_count-1 .. 0). */
+int setops_gen_kset_lens(size_t max_len, double skewness, size_t set_count,
+                         size_t *lens);
+/* gen_kset: every set contains floor(selectivity * smallest_len) shared
+ * elements and uniform fill (sorted_set_containing, generators.rs:139-215);
+ * outs[i] needs room for lens[i] from setops_gen_kset_lens. */
+int setops_gen_kset(uint64_t seed, double density, double selectivity,
+                    size_t max_len, double skewness, size_t set_count,
+                    uint32_t *const *outs);
+
+/* Batched uneven pairs: pair p has |A| and |B| each log-uniform in
+ * [min_len, max_len], density U[dmin, dmax] (max_value = max(|A|,|B|) /
+ * density) and selectivity U[smin, smax] of the smaller set.
+ * setops_gen_batch_sizes draws the lengths; setops_gen_batch_fill writes
+ * the sets into pool at the given offsets (nthreads workers; the output does
+ * not depend on nthreads). */
+int setops_gen_batch_sizes(uint64_t seed, size_t npairs, size_t min_len,
+                           size_t max_len, uint64_t *a_len, uint64_t *b_len);
+int setops_gen_batch_fill(uint64_t seed, size_t npairs, const uint64_t *a_len,
+                          const uint64_t *b_len, const uint64_t *a_off,
+                          const uint64_t *b_off, double dmin, double dmax,
+                          double smin, double smax, uint32_t *pool,
+                          int nthreads);
+
+/* Posting-list index: list r (1-based rank) has
+ * clip(floor(max_len / r^s), 1, max_len) documents drawn without
+ * replacement from [0, doc_space), sorted.  setops_gen_index_lens fills
+ * lens; setops_gen_index_fill writes the lists at offs into pool. */
+int setops_gen_index_lens(size_t nlists, size_t max_len, double s,
+                          uint64_t *lens);
+int setops_gen_index_fill(uint64_t seed, size_t nlists, const uint64_t *lens,
+                          const uint64_t *offs, uint64_t doc_space,
+                          uint32_t *pool, int nthreads);
+
+/* Sorted, duplicate-free sample of n values from [0, max_value). */
+int setops_gen_sorted_sample(uint64_t seed, size_t n, uint64_t max_value,
+                             uint32_t *out);
+
+/* ---- datafile format (benchmark/src/datafile.rs:5-166) -------------------
+ * Header: magic E9 AA 05, flag byte (bit 0 = little endian), u32 set count
+ * (>= 2); then set_count u32 lengths; then the sets as 32-bit integers.
+ * setops_datafile_write returns 0 or a negative code:
+ *   -1 bad argument, -2 I/O error, -3 bad set count.
+ * setops_datafile_read_header fills *set_count and lens (room for
+ * max_sets entries) and returns 0 or: -2 I/O, -3 bad set count, -4 bad
+ * magic, -5 bad endianness, -6 lens too small.  setops_datafile_read_sets
+ * then reads all sets into the caller's buffers. */
+int setops_datafile_write(const char *path, const uint32_t *const *sets,
+                          const uint64_t *lens, size_t set_count);
+int setops_datafile_read_header(const char *path, uint64_t *set_count,
+                                uint64_t *lens, size_t max_sets);
+int setops_datafile_read_sets(const char *path, uint32_t *const *sets);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SETOPS_BENCH_H */

@@ -1,0 +1,173 @@
+/*
+ * setops_gpu.h -- C ABI of the GB300 (sm_103a) sorted-u32 set-intersection
+ * library (libsetops_gpu.so).
+ *
+ * This is the drop-in boundary for the hot path of the Rust crate `setops`
+ * (UNSW-database/simd_set_operations).  Each entry point names the reference
+ * interface it replaces.  The existing native boundary of that crate,
+ * setops/ffi/qfilter/qfilter.h:8-39, sets the conventions kept here: plain
+ * pointers and lengths, caller-owned output buffers, the result length as the
+ * return channel.
+ *
+ * Conventions
+ *   - Sets are strictly increasing arrays of uint32_t (unsigned order).  As in
+ *     the reference, results on unsorted or duplicated input are unspecified;
+ *     setops_gpu_validate_sorted() checks an input.
+ *   - Materialising calls need out_cap >= min(|A|, |B|) (the reference's
+ *     Intersect2C / UnsafeWriter convention: setops/src/intersect.rs:54-67,
+ *     setops/src/intersect/qfilter_c.rs:11); otherwise SETOPS_ERR_CAPACITY.
+ *   - Every call returns a status (0 = OK, negative = error) instead of the
+ *     reference's assert!/abort.  setops_gpu_last_error() gives the text.
+ *   - flags: SETOPS_HOST means every set/output pointer of the call is host
+ *     memory (the call copies in and out and returns when done; pinned memory
+ *     gives full copy speed).  Without it the pointers are device pointers.
+ *     Device-pointer calls still return their length/count to host memory and
+ *     synchronise, except the *_async calls.
+ *   - A context serialises its work on one CUDA stream; calls on one context
+ *     must not overlap from several host threads.  Distinct contexts are
+ *     independent.
+ */
+#ifndef SETOPS_GPU_H
+#define SETOPS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+  SETOPS_OK = 0,
+  SETOPS_ERR_INVALID = -1,   /* bad argument (NULL pointer, k < 2, ...)       */
+  SETOPS_ERR_CAPACITY = -2,  /* output capacity below min(|A|, |B|)           */
+  SETOPS_ERR_CUDA = -3,      /* CUDA runtime error                           */
+  SETOPS_ERR_NOMEM = -4,     /* device or pinned allocation failed           */
+  SETOPS_ERR_TIMEOUT = -5,   /* a device-side wait hit its iteration limit   */
+  SETOPS_ERR_UNSORTED = -6,  /* reserved for validation failures             */
+  SETOPS_ERR_BUSY = -7,      /* serving queue full / call in progress        */
+  SETOPS_ERR_TOO_LARGE = -8, /* input larger than an entry point supports    */
+  SETOPS_ERR_NOT_READY = -9  /* serving: no completed query to return        */
+};
+
+/* ---- flags -------------------------------------------------------------- */
+#define SETOPS_HOST 0x1u             /* pointers are host memory            */
+/* Algorithm override (default: the tuned choice for the size ratio). */
+#define SETOPS_ALGO_SHIFT 8
+#define SETOPS_ALGO_MASK (0xffu << SETOPS_ALGO_SHIFT)
+#define SETOPS_ALGO_AUTO (0u << SETOPS_ALGO_SHIFT)
+#define SETOPS_ALGO_MERGE (1u << SETOPS_ALGO_SHIFT)  /* merge-path kernel    */
+#define SETOPS_ALGO_GALLOP (2u << SETOPS_ALGO_SHIFT) /* search kernel        */
+/* Variant of the chosen kernel (tile shape / probe group); 0 = default.
+ * setops_gpu_num_variants() gives the count per algorithm. */
+#define SETOPS_VARIANT_SHIFT 16
+#define SETOPS_VARIANT_MASK (0xffu << SETOPS_VARIANT_SHIFT)
+#define SETOPS_VARIANT(v) (((unsigned)(v) & 0xffu) << SETOPS_VARIANT_SHIFT)
+
+typedef struct setops_ctx setops_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on CUDA device `device` with its own stream, scratch
+ * pool and tuning table.  (The reference has no context: its functions are
+ * pure CPU functions, setops/src/intersect.rs:40-42.) */
+int setops_gpu_create(setops_ctx **out, int device);
+int setops_gpu_destroy(setops_ctx *ctx);
+/* Use an external CUDA stream (cudaStream_t) for all later work; NULL
+ * restores the context's own stream. */
+int setops_gpu_set_stream(setops_ctx *ctx, void *cuda_stream);
+void *setops_gpu_get_stream(setops_ctx *ctx);
+/* Waits for all queued work; reports device-side errors of async calls. */
+int setops_gpu_synchronize(setops_ctx *ctx);
+const char *setops_gpu_last_error(const setops_ctx *ctx);
+const char *setops_status_string(int status);
+/* Number of kernel variants of an algorithm (SETOPS_ALGO_MERGE / _GALLOP)
+ * for the given element kind (0 = u32 arrays, 1 = BSR). */
+int setops_gpu_num_variants(unsigned algo, int bsr);
+/* Number of kernels this context has launched (for launch accounting). */
+uint64_t setops_gpu_launch_count(const setops_ctx *ctx);
+/* Algorithm policy: the kernel used for pairs whose size ratio max/min lies
+ * in [2^band, 2^(band+1)), band in [0, 32); algo_flags = SETOPS_ALGO_MERGE or
+ * SETOPS_ALGO_GALLOP | SETOPS_VARIANT(v).  The autotuner writes this table;
+ * it plays the role of the reference's compile-time choice of algorithm per
+ * ISA (setops/src/intersect.rs:26-36) and the benchmark's name registry
+ * (benchmark/src/timer.rs:75-169). */
+int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
+                          unsigned algo_flags);
+int setops_gpu_get_policy(const setops_ctx *ctx, int bsr, int ratio_band,
+                          unsigned *algo_flags);
+
+/* ---- 2-set, u32 arrays --------------------------------------------------
+ * Replace `Intersect2<[u32], V> = fn(&[u32], &[u32], &mut V)`
+ * (setops/src/intersect.rs:40) with V = Counter (setops/src/visitor.rs:24)
+ * and V = VecWriter / SliceWriter / UnsafeWriter (visitor.rs:51,100,759), and
+ * `Intersect2C<[u32]>` (intersect.rs:41); results equal naive_merge
+ * (setops/src/intersect/merge.rs:7-33). */
+int setops_gpu_intersect_count(setops_ctx *ctx, const uint32_t *a, size_t na,
+                               const uint32_t *b, size_t nb, uint64_t *count,
+                               unsigned flags);
+int setops_gpu_intersect(setops_ctx *ctx, const uint32_t *a, size_t na,
+                         const uint32_t *b, size_t nb, uint32_t *out,
+                         size_t out_cap, size_t *out_len, unsigned flags);
+/* Device-only, no synchronisation: the result length (or count, when out is
+ * NULL) is written to the device word *len_dev.  Errors surface at
+ * setops_gpu_synchronize(). */
+int setops_gpu_intersect_async(setops_ctx *ctx, const uint32_t *a, size_t na,
+                               const uint32_t *b, size_t nb, uint32_t *out,
+                               size_t out_cap, uint64_t *len_dev,
+                               unsigned flags);
+
+/* ---- 2-set, BSR (base-and-state) -----------------------------------------
+ * Replace `Intersect2Bsr = fn(BsrRef, BsrRef, &mut BsrVec)`
+ * (setops/src/bsr.rs:16) and the BSR Counter (setops/src/visitor.rs:399-403);
+ * results equal branchless_merge_bsr (setops/src/intersect/merge.rs:62-87).
+ * A BSR set is SoA: bases[] strictly increasing, states[] non-zero.
+ * _count gives the element count (sum of popcount of the AND-ed states);
+ * the materialising call gives the (base, state) words with a non-zero AND,
+ * out_cap >= min(na, nb) words. */
+int setops_gpu_intersect_bsr_count(setops_ctx *ctx, const uint32_t *bases_a,
+                                   const uint32_t *states_a, size_t na,
+                                   const uint32_t *bases_b,
+                                   const uint32_t *states_b, size_t nb,
+                                   uint64_t *count, unsigned flags);
+int setops_gpu_intersect_bsr(setops_ctx *ctx, const uint32_t *bases_a,
+                             const uint32_t *states_a, size_t na,
+                             const uint32_t *bases_b, const uint32_t *states_b,
+                             size_t nb, uint32_t *out_bases,
+                             uint32_t *out_states, size_t out_cap,
+                             size_t *out_len, unsigned flags);
+/* BsrVec::from_sorted (setops/src/bsr.rs:140-163) on the device: encodes a
+ * sorted set of n elements into *nwords (base, state) words; bases/states
+ * need room for n words. */
+int setops_gpu_bsr_from_sorted(setops_ctx *ctx, const uint32_t *in, size_t n,
+                               uint32_t *bases, uint32_t *states,
+                               size_t *nwords, unsigned flags);
+/* BsrVec::to_sorted_set (setops/src/bsr.rs:77-88) on the device; out needs
+ * room for the popcount total (<= 32 * n). */
+int setops_gpu_bsr_to_sorted(setops_ctx *ctx, const uint32_t *bases,
+                             const uint32_t *states, size_t n, uint32_t *out,
+                             size_t out_cap, size_t *out_len, unsigned flags);
+
+/* ---- k-set SvS -----------------------------------------------------------
+ * Replace svs_generic (setops/src/intersect/svs.rs:50-73) / run_svs
+ * (svs.rs:103-116) and `IntersectK` (setops/src/intersect.rs:42).  Sets are
+ * intersected smallest-first (the reference assumes the caller ordered them,
+ * svs.rs:7; intersection is order-independent, so the result is the same);
+ * intermediate results stay on the device.  out_cap >= min(lens). */
+int setops_gpu_svs(setops_ctx *ctx, const uint32_t *const *sets,
+                   const size_t *lens, size_t k, uint32_t *out,
+                   size_t out_cap, size_t *out_len, unsigned flags);
+int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
+                         const size_t *lens, size_t k, uint64_t *count,
+                         unsigned flags);
+
+/* ---- validation ----------------------------------------------------------
+ * *is_sorted = 1 when a[0..n) is strictly increasing (no counterpart: the
+ * reference debug_asserts this, setops/src/bsr.rs:71-72). */
+int setops_gpu_validate_sorted(setops_ctx *ctx, const uint32_t *a, size_t n,
+                               int *is_sorted, unsigned flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SETOPS_GPU_H */

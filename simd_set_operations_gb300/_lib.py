@@ -1,0 +1,114 @@
+"""ctypes binding of libsetops_gpu.so (include/setops_gpu.h, setops_bench.h).
+
+There is no CPU fallback: if the library is missing, importing this module
+raises ImportError telling how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsetops_gpu.so"
+
+OK = 0
+ERR_INVALID = -1
+ERR_CAPACITY = -2
+ERR_CUDA = -3
+ERR_NOMEM = -4
+ERR_TIMEOUT = -5
+ERR_UNSORTED = -6
+ERR_BUSY = -7
+ERR_TOO_LARGE = -8
+ERR_NOT_READY = -9
+
+HOST = 0x1
+ALGO_SHIFT = 8
+ALGO_AUTO = 0 << ALGO_SHIFT
+ALGO_MERGE = 1 << ALGO_SHIFT
+ALGO_GALLOP = 2 << ALGO_SHIFT
+VARIANT_SHIFT = 16
+
+
+def VARIANT(v: int) -> int:
+    return (v & 0xFF) << VARIANT_SHIFT
+
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+szp = C.POINTER(C.c_size_t)
+vp = C.c_void_p
+sz = C.c_size_t
+u64 = C.c_uint64
+uint = C.c_uint
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with "
+            "`python -m simd_set_operations_gb300.build` (needs nvcc); "
+            "this package has no CPU fallback")
+    return C.CDLL(str(LIB_PATH))
+
+
+lib = _load()
+
+# (name, restype, argtypes) -- every symbol declared in include/*.h
+SIGNATURES = [
+    ("setops_status_string", C.c_char_p, [C.c_int]),
+    ("setops_gpu_create", C.c_int, [C.POINTER(vp), C.c_int]),
+    ("setops_gpu_destroy", C.c_int, [vp]),
+    ("setops_gpu_set_stream", C.c_int, [vp, vp]),
+    ("setops_gpu_get_stream", vp, [vp]),
+    ("setops_gpu_synchronize", C.c_int, [vp]),
+    ("setops_gpu_last_error", C.c_char_p, [vp]),
+    ("setops_gpu_num_variants", C.c_int, [uint, C.c_int]),
+    ("setops_gpu_launch_count", u64, [vp]),
+    ("setops_gpu_set_policy", C.c_int, [vp, C.c_int, C.c_int, uint]),
+    ("setops_gpu_get_policy", C.c_int, [vp, C.c_int, C.c_int, C.POINTER(uint)]),
+    ("setops_gpu_intersect_count", C.c_int, [vp, vp, sz, vp, sz, u64p, uint]),
+    ("setops_gpu_intersect", C.c_int, [vp, vp, sz, vp, sz, vp, sz, szp, uint]),
+    ("setops_gpu_intersect_async", C.c_int, [vp, vp, sz, vp, sz, vp, sz, vp, uint]),
+    ("setops_gpu_intersect_bsr_count", C.c_int, [vp, vp, vp, sz, vp, vp, sz, u64p, uint]),
+    ("setops_gpu_intersect_bsr", C.c_int, [vp, vp, vp, sz, vp, vp, sz, vp, vp, sz, szp, uint]),
+    ("setops_gpu_bsr_from_sorted", C.c_int, [vp, vp, sz, vp, vp, szp, uint]),
+    ("setops_gpu_bsr_to_sorted", C.c_int, [vp, vp, vp, sz, vp, sz, szp, uint]),
+    ("setops_gpu_svs", C.c_int, [vp, C.POINTER(vp), szp, sz, vp, sz, szp, uint]),
+    ("setops_gpu_svs_count", C.c_int, [vp, C.POINTER(vp), szp, sz, u64p, uint]),
+    ("setops_gpu_validate_sorted", C.c_int, [vp, vp, sz, C.POINTER(C.c_int), uint]),
+    # setops_bench.h
+    ("setops_gen_twoset", C.c_int, [u64, C.c_double, C.c_double, sz, sz, vp, vp]),
+    ("setops_gen_kset_lens", C.c_int, [sz, C.c_double, sz, szp]),
+    ("setops_gen_kset", C.c_int, [u64, C.c_double, C.c_double, sz, C.c_double, sz, C.POINTER(vp)]),
+    ("setops_gen_batch_sizes", C.c_int, [u64, sz, sz, sz, vp, vp]),
+    ("setops_gen_batch_fill", C.c_int, [u64, sz, vp, vp, vp, vp, C.c_double, C.c_double,
+                                        C.c_double, C.c_double, vp, C.c_int]),
+    ("setops_gen_index_lens", C.c_int, [sz, sz, C.c_double, vp]),
+    ("setops_gen_index_fill", C.c_int, [u64, sz, vp, vp, u64, vp, C.c_int]),
+    ("setops_gen_sorted_sample", C.c_int, [u64, sz, u64, vp]),
+    ("setops_datafile_write", C.c_int, [C.c_char_p, C.POINTER(vp), vp, sz]),
+    ("setops_datafile_read_header", C.c_int, [C.c_char_p, u64p, vp, sz]),
+    ("setops_datafile_read_sets", C.c_int, [C.c_char_p, C.POINTER(vp)]),
+]
+
+
+def _bind() -> None:
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)  # AttributeError if the library lacks it
+        fn.restype = res
+        fn.argtypes = args
+
+
+_bind()
+
+
+class SetopsError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+def status_string(status: int) -> str:
+    return lib.setops_status_string(status).decode()

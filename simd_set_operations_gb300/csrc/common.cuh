@@ -1,0 +1,216 @@
+// common.cuh -- device helpers shared by the set-intersection kernels.
+//
+// * mbarrier + cp.async.bulk (1-D TMA) wrappers for staging input windows in
+//   shared memory (sm_90+ PTX; this library is built for sm_103a only);
+// * bounded spin-waits: every wait has an iteration limit, after which the
+//   kernel records an error code in global memory and returns instead of
+//   hanging the GPU;
+// * decoupled look-back over an epoch-tagged status array, used to turn
+//   per-tile match counts into global output offsets in a single pass.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace setops {
+
+// Error codes a kernel can record in its error word (first writer wins).
+enum DeviceError : int {
+  DEV_OK = 0,
+  DEV_ERR_TIMEOUT_MBAR = 1,      // a bulk-copy barrier never completed
+  DEV_ERR_TIMEOUT_LOOKBACK = 2,  // a predecessor tile never published
+  DEV_ERR_CAPACITY = 3,          // output would exceed its capacity
+};
+
+// Spin limits.  A try_wait returns after a short hardware time slice, so the
+// mbarrier limit corresponds to well over a second of waiting.
+constexpr uint32_t kMbarSpinLimit = 1u << 24;
+constexpr uint32_t kLookbackSpinLimit = 1u << 26;
+
+__device__ __forceinline__ void record_error(int *err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- mbarrier ------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
+                                                      uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for phase `parity` of `bar` to complete.  Returns false (and records
+// DEV_ERR_TIMEOUT_MBAR) if the limit is reached.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
+                                                  uint32_t parity, int *err) {
+  for (uint32_t it = 0; it < kMbarSpinLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+  record_error(err, DEV_ERR_TIMEOUT_MBAR);
+  return false;
+}
+
+// 1-D bulk copy global -> shared, completing `bytes` on `bar`.  dst, src and
+// bytes must be multiples of 16.  The evict-first L2 policy marks the
+// streamed inputs as read-once.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         uint32_t bytes, uint64_t *bar,
+                                         uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes."
+      "L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;"
+               : "=l"(pol));
+  return pol;
+}
+
+// ---- global status words -------------------------------------------------
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t *p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];"
+               : "=l"(v)
+               : "l"(p)
+               : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_u64(uint64_t *p, uint64_t v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v)
+               : "memory");
+}
+
+// Look-back status word: [63:48] epoch (launch tag), [47:46] flag,
+// [45:0] value.  Entries from earlier launches carry another epoch and read
+// as "not yet published", so the array never needs clearing between launches.
+constexpr uint64_t kFlagAggregate = 1;
+constexpr uint64_t kFlagPrefix = 2;
+constexpr uint64_t kValueMask = (uint64_t(1) << 46) - 1;
+
+__device__ __forceinline__ uint64_t pack_status(uint32_t epoch, uint64_t flag,
+                                                uint64_t value) {
+  return (uint64_t(epoch & 0xffffu) << 48) | (flag << 46) | (value & kValueMask);
+}
+
+// Decoupled look-back (single thread).  Publishes `aggregate` for `tile`,
+// walks predecessors until an inclusive prefix is found, publishes this
+// tile's inclusive prefix and returns the exclusive prefix.  Tiles must have
+// been started in increasing order (tile ids come from an atomic ticket), so
+// every predecessor is running or finished and the walk terminates; the spin
+// is bounded anyway.  Returns UINT64_MAX on timeout (error recorded).
+__device__ __forceinline__ uint64_t lookback_exclusive(uint64_t *status,
+                                                       uint32_t tile,
+                                                       uint64_t aggregate,
+                                                       uint32_t epoch,
+                                                       int *err) {
+  if (tile == 0) {
+    st_release_u64(&status[0], pack_status(epoch, kFlagPrefix, aggregate));
+    return 0;
+  }
+  st_release_u64(&status[tile], pack_status(epoch, kFlagAggregate, aggregate));
+  uint64_t excl = 0;
+  int64_t t = int64_t(tile) - 1;
+  uint32_t spins = 0;
+  while (t >= 0) {
+    uint64_t w = ld_acquire_u64(&status[t]);
+    uint32_t e = uint32_t(w >> 48);
+    uint64_t flag = (w >> 46) & 3;
+    if (e != (epoch & 0xffffu) || flag == 0) {
+      if (++spins > kLookbackSpinLimit) {
+        record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
+        return UINT64_MAX;
+      }
+      continue;
+    }
+    excl += (w & kValueMask);
+    if (flag == kFlagPrefix) break;
+    --t;
+  }
+  st_release_u64(&status[tile],
+                 pack_status(epoch, kFlagPrefix, excl + aggregate));
+  return excl;
+}
+
+// True when a kernel with device-side choice rule `rule` should not run for
+// lengths (na, nb): rule 1 runs only when max/min >= thr, rule 2 only below.
+// An empty input counts as "search" (either kernel returns 0).
+__device__ __forceinline__ bool skip_by_rule(int rule, uint32_t thr,
+                                             uint64_t na, uint64_t nb) {
+  if (rule == 0) return false;
+  const uint64_t mn = na < nb ? na : nb, mx = na < nb ? nb : na;
+  const bool search = (mn == 0) || (mx / mn >= uint64_t(thr));
+  return (rule == 1) ? !search : search;
+}
+
+// Per-launch coordination words kept in scratch (zeroed once at allocation;
+// the last CTA of every launch restores them to zero).
+struct LaunchSync {
+  uint32_t ticket;  // next virtual CTA / tile id
+  uint32_t done;    // CTAs finished
+  unsigned long long acc;  // count accumulator (count-only kernels)
+};
+
+// Block-wide exclusive scan of one uint32 per thread.  `warp_sums` needs
+// NT/32 entries of shared memory.  Returns the exclusive prefix; *total gets
+// the block total.  Contains __syncthreads(); call from all threads.
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v,
+                                                         uint32_t *warp_sums,
+                                                         uint32_t *total) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  uint32_t wpre = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    uint32_t s = warp_sums[w];
+    wpre += (w < warp) ? s : 0u;
+    tot += s;
+  }
+  __syncthreads();
+  *total = tot;
+  return wpre + x - v;
+}
+
+}  // namespace setops

@@ -1,0 +1,266 @@
+// kernels.cu -- instantiation table of the intersection kernels, plus the
+// small utility kernels (sortedness check, device BSR encode / decode).
+#include "kernels.h"
+
+#include "gallop.cuh"
+#include "merge.cuh"
+
+namespace setops {
+
+namespace {
+
+template <int NT, int VT, int RLOG, bool BSR, bool MAT>
+KernelInfo mk_merge(const char *name) {
+  return KernelInfo{reinterpret_cast<const void *>(
+                        &merge_kernel<NT, VT, RLOG, BSR, MAT>),
+                    NT, MergeCfg<NT, VT, RLOG, BSR, MAT>::kSmemBytes, NT * VT,
+                    name};
+}
+
+template <int NT, int GS, int ITEMS, int NSAMP, bool BSR, bool MAT>
+KernelInfo mk_gallop(const char *name) {
+  return KernelInfo{reinterpret_cast<const void *>(
+                        &gallop_kernel<NT, GS, ITEMS, NSAMP, BSR, MAT>),
+                    NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name};
+}
+
+// [variant][count, materialise]
+#define MERGE_ROW(NT, VT, RL, BSR)                                   \
+  {mk_merge<NT, VT, RL, BSR, false>("merge_" #NT "x" #VT "_r" #RL),  \
+   mk_merge<NT, VT, RL, BSR, true>("merge_" #NT "x" #VT "_r" #RL)}
+#define GALLOP_ROW(NT, GS, IT, BSR)                                       \
+  {mk_gallop<NT, GS, IT, 2048, BSR, false>("gallop_" #NT "_g" #GS "_i" #IT), \
+   mk_gallop<NT, GS, IT, 2048, BSR, true>("gallop_" #NT "_g" #GS "_i" #IT)}
+
+const KernelInfo kMergeU32[][2] = {
+    MERGE_ROW(256, 8, 13, false),   // 0: NV 2048, 64 KB rings
+    MERGE_ROW(128, 16, 13, false),  // 1: NV 2048, fewer threads, longer runs
+    MERGE_ROW(256, 4, 12, false),   // 2: NV 1024, 32 KB rings
+    MERGE_ROW(512, 4, 13, false),   // 3: NV 2048, 16 warps
+    MERGE_ROW(128, 8, 12, false),   // 4: NV 1024, 4 warps
+};
+const KernelInfo kMergeBsr[][2] = {
+    MERGE_ROW(128, 8, 12, true),   // 0: NV 1024, 64 KB rings
+    MERGE_ROW(256, 4, 12, true),   // 1
+    MERGE_ROW(256, 8, 13, true),   // 2: NV 2048, 128 KB rings
+};
+const KernelInfo kGallopU32[][2] = {
+    GALLOP_ROW(256, 1, 4, false),   // 0: thread per element, 4 interleaved
+    GALLOP_ROW(256, 4, 2, false),   // 1
+    GALLOP_ROW(256, 8, 1, false),   // 2
+    GALLOP_ROW(256, 32, 1, false),  // 3: warp per element
+    GALLOP_ROW(128, 32, 1, false),  // 4
+    GALLOP_ROW(256, 1, 1, false),   // 5
+};
+const KernelInfo kGallopBsr[][2] = {
+    GALLOP_ROW(256, 1, 4, true),
+    GALLOP_ROW(256, 8, 1, true),
+    GALLOP_ROW(256, 32, 1, true),
+};
+
+template <class T, size_t N>
+constexpr int count_of(const T (&)[N]) {
+  return int(N);
+}
+
+}  // namespace
+
+int num_variants(Algo algo, bool bsr) {
+  if (algo == ALGO_MERGE) return bsr ? count_of(kMergeBsr) : count_of(kMergeU32);
+  return bsr ? count_of(kGallopBsr) : count_of(kGallopU32);
+}
+
+const KernelInfo &variant(Algo algo, bool bsr, bool mat, int v) {
+  const int n = num_variants(algo, bsr);
+  if (v < 0 || v >= n) v = 0;
+  const int m = mat ? 1 : 0;
+  if (algo == ALGO_MERGE) return bsr ? kMergeBsr[v][m] : kMergeU32[v][m];
+  return bsr ? kGallopBsr[v][m] : kGallopU32[v][m];
+}
+
+// ---------------------------------------------------------------------------
+// Sortedness check: flag := 1 if some a[i] >= a[i+1].
+__global__ void validate_sorted_kernel(const uint32_t *a, uint64_t n,
+                                       int *flag) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  bool bad = false;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i + 1 < n;
+       i += stride)
+    bad |= __ldg(a + i) >= __ldg(a + i + 1);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+cudaError_t launch_validate_sorted(const uint32_t *a, uint64_t n, int *flag,
+                                   int sms, cudaStream_t st) {
+  uint64_t blocks = (n + kUtilThreads * 8 - 1) / (kUtilThreads * 8);
+  if (blocks > uint64_t(sms) * 8) blocks = uint64_t(sms) * 8;
+  if (blocks < 1) blocks = 1;
+  validate_sorted_kernel<<<unsigned(blocks), kUtilThreads, 0, st>>>(a, n, flag);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// BsrVec::from_sorted (setops/src/bsr.rs:140-163) on the device.  Tiles of
+// kBsrEncodeTile elements have their edges moved forward to the next base
+// change (a base holds at most 32 elements), so every word belongs to exactly
+// one tile; word offsets come from decoupled look-back.
+__device__ __forceinline__ uint64_t next_word_start(const uint32_t *in,
+                                                    uint64_t n, uint64_t i) {
+  if (i == 0 || i >= n) return i < n ? i : n;
+  while (i < n && (__ldg(in + i) >> 5) == (__ldg(in + i - 1) >> 5)) ++i;
+  return i;
+}
+
+__global__ void __launch_bounds__(kUtilThreads)
+    bsr_encode_kernel(const uint32_t *in, uint64_t n, uint32_t *bases,
+                      uint32_t *states, uint64_t *nwords, uint64_t *status,
+                      LaunchSync *sync, int *err, uint32_t epoch) {
+  constexpr int NT = kUtilThreads;
+  __shared__ uint32_t warp_sums[NT / 32];
+  __shared__ uint32_t s_tile;
+  __shared__ unsigned long long s_rng[2];
+  __shared__ unsigned long long s_excl;
+  const int t = threadIdx.x;
+  const uint64_t ntiles = (n + kBsrEncodeTile - 1) / kBsrEncodeTile;
+  for (;;) {
+    if (t == 0) {
+      s_tile = atomicAdd(&sync->ticket, 1u);
+      if (uint64_t(s_tile) < ntiles) {
+        const uint64_t s = uint64_t(s_tile) * kBsrEncodeTile;
+        const uint64_t e = s + kBsrEncodeTile < n ? s + kBsrEncodeTile : n;
+        s_rng[0] = next_word_start(in, n, s);
+        s_rng[1] = next_word_start(in, n, e);
+      }
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (uint64_t(tile) >= ntiles) break;
+    const uint64_t s = s_rng[0], e = s_rng[1];
+    const uint64_t len = e > s ? e - s : 0;
+    const uint64_t chunk = (len + NT - 1) / NT;
+    const uint64_t cs = s + chunk * t < e ? s + chunk * t : e;
+    const uint64_t ce = cs + chunk < e ? cs + chunk : e;
+    uint32_t starts = 0;
+    for (uint64_t i = cs; i < ce; ++i)
+      starts += (i == 0) || ((__ldg(in + i) >> 5) != (__ldg(in + i - 1) >> 5));
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<NT>(starts, warp_sums, &tot);
+    if (t == 0) s_excl = lookback_exclusive(status, tile, tot, epoch, err);
+    __syncthreads();
+    const uint64_t tex = s_excl;
+    if (tex == UINT64_MAX) return;
+    uint64_t w = tex + ex;
+    for (uint64_t i = cs; i < ce; ++i) {
+      const uint32_t v = __ldg(in + i);
+      if (i != 0 && (v >> 5) == (__ldg(in + i - 1) >> 5)) continue;
+      const uint32_t base = v >> 5;
+      uint32_t state = 1u << (v & 31u);
+      for (uint64_t j = i + 1; j < e; ++j) {
+        const uint32_t u = __ldg(in + j);
+        if ((u >> 5) != base) break;
+        state |= 1u << (u & 31u);
+      }
+      bases[w] = base;
+      states[w] = state;
+      ++w;
+    }
+    if (tile == ntiles - 1 && t == 0) *nwords = tex + tot;
+    __syncthreads();
+  }
+  if (t == 0) {
+    __threadfence();
+    if (atomicAdd(&sync->done, 1u) == gridDim.x - 1) {
+      if (ntiles == 0) *nwords = 0;
+      sync->ticket = 0;
+      sync->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+// BsrVec::to_sorted_set (setops/src/bsr.rs:77-88) on the device.
+__global__ void __launch_bounds__(kUtilThreads)
+    bsr_decode_kernel(const uint32_t *bases, const uint32_t *states,
+                      uint64_t n, uint32_t *out, uint64_t out_cap,
+                      uint64_t *out_len, uint64_t *status, LaunchSync *sync,
+                      int *err, uint32_t epoch) {
+  constexpr int NT = kUtilThreads;
+  constexpr int WPT = kBsrDecodeTile / NT;
+  __shared__ uint32_t warp_sums[NT / 32];
+  __shared__ uint32_t s_tile;
+  __shared__ unsigned long long s_excl;
+  const int t = threadIdx.x;
+  const uint64_t ntiles = (n + kBsrDecodeTile - 1) / kBsrDecodeTile;
+  for (;;) {
+    if (t == 0) s_tile = atomicAdd(&sync->ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (uint64_t(tile) >= ntiles) break;
+    const uint64_t w0 = uint64_t(tile) * kBsrDecodeTile + uint64_t(t) * WPT;
+    uint32_t mine = 0;
+#pragma unroll
+    for (int q = 0; q < WPT; ++q)
+      if (w0 + q < n) mine += __popc(__ldg(states + w0 + q));
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<NT>(mine, warp_sums, &tot);
+    if (t == 0) s_excl = lookback_exclusive(status, tile, tot, epoch, err);
+    __syncthreads();
+    const uint64_t tex = s_excl;
+    if (tex == UINT64_MAX) return;
+    if (tex + tot > out_cap) {
+      if (t == 0) record_error(err, DEV_ERR_CAPACITY);
+      return;
+    }
+    uint64_t o = tex + ex;
+#pragma unroll
+    for (int q = 0; q < WPT; ++q) {
+      if (w0 + q >= n) break;
+      const uint32_t hi = __ldg(bases + w0 + q) << 5;
+      uint32_t s = __ldg(states + w0 + q);
+      while (s) {
+        out[o++] = hi | uint32_t(__ffs(s) - 1);
+        s &= s - 1;
+      }
+    }
+    if (tile == ntiles - 1 && t == 0) *out_len = tex + tot;
+    __syncthreads();
+  }
+  if (t == 0) {
+    __threadfence();
+    if (atomicAdd(&sync->done, 1u) == gridDim.x - 1) {
+      if (ntiles == 0) *out_len = 0;
+      sync->ticket = 0;
+      sync->done = 0;
+      __threadfence();
+    }
+  }
+}
+
+const void *bsr_encode_fn() {
+  return reinterpret_cast<const void *>(&bsr_encode_kernel);
+}
+const void *bsr_decode_fn() {
+  return reinterpret_cast<const void *>(&bsr_decode_kernel);
+}
+
+cudaError_t launch_bsr_encode(const uint32_t *in, uint64_t n, uint32_t *bases,
+                              uint32_t *states, uint64_t *nwords,
+                              uint64_t *status, LaunchSync *sync, int *err,
+                              uint32_t epoch, int grid, cudaStream_t st) {
+  bsr_encode_kernel<<<grid, kUtilThreads, 0, st>>>(in, n, bases, states,
+                                                   nwords, status, sync, err,
+                                                   epoch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bsr_decode(const uint32_t *bases, const uint32_t *states,
+                              uint64_t n, uint32_t *out, uint64_t out_cap,
+                              uint64_t *out_len, uint64_t *status,
+                              LaunchSync *sync, int *err, uint32_t epoch,
+                              int grid, cudaStream_t st) {
+  bsr_decode_kernel<<<grid, kUtilThreads, 0, st>>>(
+      bases, states, n, out, out_cap, out_len, status, sync, err, epoch);
+  return cudaGetLastError();
+}
+
+}  // namespace setops

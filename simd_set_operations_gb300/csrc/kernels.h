@@ -1,0 +1,50 @@
+// kernels.h -- host-side view of the compiled kernel variants.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace setops {
+
+struct MergeArgs;
+struct GallopArgs;
+
+// One compiled kernel: entry point, block size, dynamic shared memory, and
+// the number of merged elements (merge) or small-set elements (search) one
+// tile covers.
+struct KernelInfo {
+  const void *fn;
+  int nt;
+  size_t dyn_smem;
+  int tile;
+  const char *name;
+};
+
+enum Algo { ALGO_MERGE = 1, ALGO_GALLOP = 2 };
+
+int num_variants(Algo algo, bool bsr);
+// kind: 0 count, 1 materialise
+const KernelInfo &variant(Algo algo, bool bsr, bool mat, int v);
+
+// Utility kernels (launch on `st`).
+cudaError_t launch_validate_sorted(const uint32_t *a, uint64_t n, int *flag,
+                                   int sms, cudaStream_t st);
+cudaError_t launch_bsr_encode(const uint32_t *in, uint64_t n, uint32_t *bases,
+                              uint32_t *states, uint64_t *nwords,
+                              uint64_t *status, LaunchSync *sync, int *err,
+                              uint32_t epoch, int grid, cudaStream_t st);
+cudaError_t launch_bsr_decode(const uint32_t *bases, const uint32_t *states,
+                              uint64_t n, uint32_t *out, uint64_t out_cap,
+                              uint64_t *out_len, uint64_t *status,
+                              LaunchSync *sync, int *err, uint32_t epoch,
+                              int grid, cudaStream_t st);
+constexpr int kBsrEncodeTile = 256 * 8;  // elements per encode tile
+constexpr int kBsrDecodeTile = 256 * 4;  // words per decode tile
+const void *bsr_encode_fn();
+const void *bsr_decode_fn();
+constexpr int kUtilThreads = 256;
+
+}  // namespace setops

@@ -1,0 +1,858 @@
+// runtime.cu -- host runtime behind the C ABI (include/setops_gpu.h):
+// context, scratch pool, algorithm choice, kernel launches, and the k-set
+// SvS driver that keeps intermediates on the device.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/setops_gpu.h"
+#include "gallop.cuh"
+#include "kernels.h"
+#include "merge.cuh"
+#include "runtime.h"
+
+using namespace setops;
+
+// ---------------------------------------------------------------------------
+// context helpers
+
+namespace {
+
+const char *kStatusText[] = {
+    "ok",          "invalid argument", "output capacity too small",
+    "CUDA error",  "out of memory",    "device wait timed out",
+    "unsorted input", "busy",          "input too large",
+    "not ready"};
+
+}  // namespace
+
+int ctx_fail(setops_ctx *ctx, int status, const std::string &what) {
+  if (ctx) ctx->err = what;
+  return status;
+}
+
+int ctx_cuda(setops_ctx *ctx, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return SETOPS_OK;
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation)
+    return ctx_fail(ctx, SETOPS_ERR_NOMEM, msg);
+  return ctx_fail(ctx, SETOPS_ERR_CUDA, msg);
+}
+
+#define CK(call)                                                     \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) return ctx_cuda(ctx, e_, #call);          \
+  } while (0)
+#define RK(call)                 \
+  do {                           \
+    int r_ = (call);             \
+    if (r_ != SETOPS_OK) return r_; \
+  } while (0)
+
+int buf_reserve(setops_ctx *ctx, DevBuf &b, size_t bytes) {
+  if (bytes <= b.cap) return SETOPS_OK;
+  size_t want = std::max<size_t>(bytes, 4096);
+  want = std::max(want, b.cap + b.cap / 2);  // grow geometrically
+  if (b.p) {
+    CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaFree(b.p));
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&b.p, bytes);  // retry at the exact size
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      b.p = nullptr;
+      return ctx_fail(ctx, SETOPS_ERR_NOMEM,
+                      "device allocation of " + std::to_string(bytes) +
+                          " bytes failed");
+    }
+    want = bytes;
+  }
+  b.cap = want;
+  return SETOPS_OK;
+}
+
+// Blocks per SM of a kernel at its launch shape (cached), also raising the
+// dynamic shared-memory limit the first time.
+int ctx_occupancy(setops_ctx *ctx, const KernelInfo &k, int *blocks) {
+  auto it = ctx->occ.find(k.fn);
+  if (it != ctx->occ.end()) {
+    *blocks = it->second;
+    return SETOPS_OK;
+  }
+  if (k.dyn_smem > 48 * 1024)
+    CK(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(k.dyn_smem)));
+  int n = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k.fn, k.nt, k.dyn_smem));
+  if (n < 1) n = 1;
+  ctx->occ[k.fn] = n;
+  *blocks = n;
+  return SETOPS_OK;
+}
+
+// Next launch tag for look-back status words; wraps within 16 bits, and the
+// status array is cleared whenever the tag wraps so that stale words of an
+// earlier launch with the same tag cannot be mistaken for fresh ones.
+int ctx_next_epoch(setops_ctx *ctx, uint32_t *epoch) {
+  ctx->epoch = (ctx->epoch + 1) & 0xffffu;
+  if (ctx->epoch == 0) {
+    if (ctx->status.p)
+      CK(cudaMemsetAsync(ctx->status.p, 0, ctx->status.cap, ctx->st));
+    ctx->epoch = 1;
+  }
+  *epoch = ctx->epoch;
+  return SETOPS_OK;
+}
+
+int ctx_status_words(setops_ctx *ctx, uint64_t n) {
+  const size_t need = size_t(std::max<uint64_t>(n, 1)) * sizeof(uint64_t);
+  if (need <= ctx->status.cap) return SETOPS_OK;
+  const size_t old = ctx->status.cap;
+  RK(buf_reserve(ctx, ctx->status, need));
+  (void)old;
+  CK(cudaMemsetAsync(ctx->status.p, 0, ctx->status.cap, ctx->st));
+  return SETOPS_OK;
+}
+
+// Device error word -> status; clears device state after an error so the
+// next call starts clean.
+int ctx_check_device(setops_ctx *ctx) {
+  CK(cudaMemcpyAsync(&ctx->hres[15], ctx->derr, sizeof(int),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  int code = 0;
+  std::memcpy(&code, &ctx->hres[15], sizeof(int));
+  if (code == 0) return SETOPS_OK;
+  CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->st));
+  CK(cudaMemsetAsync(ctx->sync, 0, sizeof(LaunchSync) * kSyncSlots, ctx->st));
+  if (ctx->status.p)
+    CK(cudaMemsetAsync(ctx->status.p, 0, ctx->status.cap, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  switch (code) {
+    case DEV_ERR_CAPACITY:
+      return ctx_fail(ctx, SETOPS_ERR_CAPACITY,
+                      "device: output would exceed its capacity");
+    case DEV_ERR_TIMEOUT_MBAR:
+      return ctx_fail(ctx, SETOPS_ERR_TIMEOUT,
+                      "device: bulk-copy barrier wait hit its limit");
+    case DEV_ERR_TIMEOUT_LOOKBACK:
+      return ctx_fail(ctx, SETOPS_ERR_TIMEOUT,
+                      "device: look-back wait hit its limit");
+    default:
+      return ctx_fail(ctx, SETOPS_ERR_CUDA,
+                      "device error code " + std::to_string(code));
+  }
+}
+
+// Reads a device u64 into *out (synchronises) and checks the error word.
+int ctx_read_u64(setops_ctx *ctx, const uint64_t *dev, uint64_t *out) {
+  CK(cudaMemcpyAsync(&ctx->hres[0], dev, sizeof(uint64_t),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  RK(ctx_check_device(ctx));
+  *out = ctx->hres[0];
+  return SETOPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// algorithm choice
+
+Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
+                  unsigned flags) {
+  Choice c;
+  const unsigned algo = (flags & SETOPS_ALGO_MASK);
+  const int var = int((flags & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+  if (algo == SETOPS_ALGO_MERGE) {
+    c.algo = ALGO_MERGE;
+    c.variant = var;
+    return c;
+  }
+  if (algo == SETOPS_ALGO_GALLOP) {
+    c.algo = ALGO_GALLOP;
+    c.variant = var;
+    return c;
+  }
+  const uint64_t mn = std::min(na, nb), mx = std::max(na, nb);
+  if (mn == 0) {
+    c.algo = ALGO_GALLOP;
+    c.variant = 0;
+    return c;
+  }
+  int band = 0;
+  for (uint64_t r = mx / mn; r > 1 && band < kRatioBands - 1; r >>= 1) ++band;
+  const unsigned pol = ctx->policy[bsr ? 1 : 0][band];
+  c.algo = ((pol & SETOPS_ALGO_MASK) == SETOPS_ALGO_GALLOP) ? ALGO_GALLOP
+                                                             : ALGO_MERGE;
+  c.variant = int((pol & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+  return c;
+}
+
+// Smallest power-of-two ratio at which the policy switches to the search
+// kernel (used for device-side choices).
+uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
+  for (int band = 0; band < kRatioBands; ++band)
+    if ((ctx->policy[bsr ? 1 : 0][band] & SETOPS_ALGO_MASK) ==
+        SETOPS_ALGO_GALLOP)
+      return 1u << band;
+  return 0xffffffffu;
+}
+
+void ctx_default_policy(setops_ctx *ctx) {
+  for (int b = 0; b < kRatioBands; ++b) {
+    // ratio < 32: merge-path; 32..511: thread-per-element search with four
+    // interleaved lookups; >= 512: one warp per element.
+    unsigned u = (b < 5)   ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
+                 : (b < 9) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
+                           : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3));
+    unsigned s = (b < 5)   ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
+                 : (b < 9) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
+                           : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
+    ctx->policy[0][b] = u;
+    ctx->policy[1][b] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// one 2-set launch (device pointers)
+
+int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
+  const uint64_t na_ub = j.na, nb_ub = j.nb;
+  const uint64_t mn = std::min(na_ub, nb_ub);
+  const bool mat = j.out != nullptr;
+  const KernelInfo &k = variant(j.choice.algo, j.bsr, mat, j.choice.variant);
+  int occ = 1;
+  RK(ctx_occupancy(ctx, k, &occ));
+  const uint64_t full = uint64_t(occ) * uint64_t(ctx->sms);
+  uint64_t grid = 1, status_words = 1;
+  if (j.choice.algo == ALGO_MERGE) {
+    const uint64_t total = na_ub + nb_ub;
+    const uint64_t per = uint64_t(k.tile) * kMinTilesPerCta;
+    grid = std::max<uint64_t>(1, std::min(full, (total + per - 1) / per));
+    status_words = grid;
+  } else {
+    const uint64_t ntiles = (mn + k.tile - 1) / k.tile;
+    grid = std::max<uint64_t>(1, std::min(full, ntiles));
+    status_words = std::max<uint64_t>(ntiles, 1);
+  }
+  if (j.grid_cap && grid > j.grid_cap) grid = j.grid_cap;
+  uint32_t epoch = 0;
+  if (mat) RK(ctx_status_words(ctx, status_words));
+  RK(ctx_next_epoch(ctx, &epoch));
+  LaunchSync *sync = ctx->sync + j.sync_slot;
+
+  if (j.choice.algo == ALGO_MERGE) {
+    MergeArgs a{};
+    a.a = j.a;
+    a.b = j.b;
+    a.sa = j.sa;
+    a.sb = j.sb;
+    a.na = j.na;
+    a.nb = j.nb;
+    a.na_dev = j.na_dev;
+    a.nb_dev = j.nb_dev;
+    if (mat) {
+      RK(buf_reserve(ctx, ctx->stage0, std::max<uint64_t>(mn, 1) * 4));
+      a.stage = static_cast<uint32_t *>(ctx->stage0.p);
+      if (j.bsr) {
+        RK(buf_reserve(ctx, ctx->stage1, std::max<uint64_t>(mn, 1) * 4));
+        a.stage_s = static_cast<uint32_t *>(ctx->stage1.p);
+      }
+    }
+    a.out = j.out;
+    a.out_s = j.out_s;
+    a.out_cap = j.out_cap;
+    a.out_len = j.len_dev;
+    a.status = static_cast<uint64_t *>(ctx->status.p);
+    a.sync = sync;
+    a.err = ctx->derr;
+    a.epoch = epoch;
+    a.skip_rule = j.skip_rule;
+    a.ratio_thr = j.ratio_thr;
+    void *args[] = {&a};
+    CK(cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args,
+                        k.dyn_smem, ctx->st));
+  } else {
+    GallopArgs a{};
+    a.a = j.a;
+    a.b = j.b;
+    a.sa = j.sa;
+    a.sb = j.sb;
+    a.na = j.na;
+    a.nb = j.nb;
+    a.na_dev = j.na_dev;
+    a.nb_dev = j.nb_dev;
+    a.out = j.out;
+    a.out_s = j.out_s;
+    a.out_cap = j.out_cap;
+    a.out_len = j.len_dev;
+    a.status = static_cast<uint64_t *>(ctx->status.p);
+    a.sync = sync;
+    a.err = ctx->derr;
+    a.epoch = epoch;
+    a.skip_rule = j.skip_rule;
+    a.ratio_thr = j.ratio_thr;
+    void *args[] = {&a};
+    CK(cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args,
+                        k.dyn_smem, ctx->st));
+  }
+  ctx->launches++;
+  return SETOPS_OK;
+}
+
+// Copies host arrays into staging slot `slot` and returns the device pointer.
+int ctx_stage_in(setops_ctx *ctx, int slot, const uint32_t *h, size_t n,
+                 const uint32_t **d) {
+  if (n == 0) {
+    *d = nullptr;
+    return SETOPS_OK;
+  }
+  RK(buf_reserve(ctx, ctx->in[slot], n * 4));
+  CK(cudaMemcpyAsync(ctx->in[slot].p, h, n * 4, cudaMemcpyHostToDevice,
+                     ctx->st));
+  *d = static_cast<const uint32_t *>(ctx->in[slot].p);
+  return SETOPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+const char *setops_status_string(int status) {
+  if (status > 0 || status < -9) return "unknown status";
+  return kStatusText[-status];
+}
+
+int setops_gpu_create(setops_ctx **out, int device) {
+  if (!out) return SETOPS_ERR_INVALID;
+  *out = nullptr;
+  setops_ctx *ctx = new (std::nothrow) setops_ctx();
+  if (!ctx) return SETOPS_ERR_NOMEM;
+  ctx->device = device;
+  int rc = SETOPS_OK;
+  do {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "cudaSetDevice"); break; }
+    e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "sm count"); break; }
+    e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "stream"); break; }
+    ctx->st = ctx->own;
+    // device scalars: [sync slots][err + flag][len words]
+    const size_t bytes = sizeof(LaunchSync) * kSyncSlots + 64 +
+                         sizeof(uint64_t) * kLenWords;
+    e = cudaMalloc(&ctx->dsmall, bytes);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "scalars"); break; }
+    e = cudaMemset(ctx->dsmall, 0, bytes);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "memset"); break; }
+    char *p = static_cast<char *>(ctx->dsmall);
+    ctx->sync = reinterpret_cast<LaunchSync *>(p);
+    p += sizeof(LaunchSync) * kSyncSlots;
+    ctx->derr = reinterpret_cast<int *>(p);
+    ctx->dflag = reinterpret_cast<int *>(p + 32);
+    p += 64;
+    ctx->dlen = reinterpret_cast<uint64_t *>(p);
+    e = cudaMallocHost(&ctx->hres, sizeof(uint64_t) * 16);
+    if (e != cudaSuccess) { rc = ctx_cuda(ctx, e, "pinned scalars"); break; }
+    ctx_default_policy(ctx);
+  } while (0);
+  if (rc != SETOPS_OK) {
+    std::fprintf(stderr, "setops_gpu_create: %s\n", ctx->err.c_str());
+    setops_gpu_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return SETOPS_OK;
+}
+
+int setops_gpu_destroy(setops_ctx *ctx) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  for (DevBuf *b : ctx->all_bufs())
+    if (b->p) cudaFree(b->p);
+  if (ctx->dsmall) cudaFree(ctx->dsmall);
+  if (ctx->hres) cudaFreeHost(ctx->hres);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return SETOPS_OK;
+}
+
+int setops_gpu_set_stream(setops_ctx *ctx, void *stream) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  CK(cudaStreamSynchronize(ctx->st));
+  ctx->st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+  return SETOPS_OK;
+}
+
+void *setops_gpu_get_stream(setops_ctx *ctx) {
+  return ctx ? static_cast<void *>(ctx->st) : nullptr;
+}
+
+int setops_gpu_synchronize(setops_ctx *ctx) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  CK(cudaStreamSynchronize(ctx->st));
+  return ctx_check_device(ctx);
+}
+
+const char *setops_gpu_last_error(const setops_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : "no context";
+}
+
+int setops_gpu_num_variants(unsigned algo, int bsr) {
+  if ((algo & SETOPS_ALGO_MASK) == SETOPS_ALGO_MERGE)
+    return num_variants(ALGO_MERGE, bsr != 0);
+  if ((algo & SETOPS_ALGO_MASK) == SETOPS_ALGO_GALLOP)
+    return num_variants(ALGO_GALLOP, bsr != 0);
+  return 0;
+}
+
+uint64_t setops_gpu_launch_count(const setops_ctx *ctx) {
+  return ctx ? ctx->launches : 0;
+}
+
+int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
+                          unsigned algo_flags) {
+  if (!ctx || ratio_band < 0 || ratio_band >= kRatioBands) return SETOPS_ERR_INVALID;
+  const unsigned a = algo_flags & SETOPS_ALGO_MASK;
+  if (a != SETOPS_ALGO_MERGE && a != SETOPS_ALGO_GALLOP) return SETOPS_ERR_INVALID;
+  const int v = int((algo_flags & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+  if (v >= num_variants(a == SETOPS_ALGO_MERGE ? ALGO_MERGE : ALGO_GALLOP, bsr != 0))
+    return SETOPS_ERR_INVALID;
+  ctx->policy[bsr ? 1 : 0][ratio_band] =
+      algo_flags & (SETOPS_ALGO_MASK | SETOPS_VARIANT_MASK);
+  return SETOPS_OK;
+}
+
+int setops_gpu_get_policy(const setops_ctx *ctx, int bsr, int ratio_band,
+                          unsigned *algo_flags) {
+  if (!ctx || !algo_flags || ratio_band < 0 || ratio_band >= kRatioBands)
+    return SETOPS_ERR_INVALID;
+  *algo_flags = ctx->policy[bsr ? 1 : 0][ratio_band];
+  return SETOPS_OK;
+}
+
+// ---- 2-set arrays ----
+
+static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
+                          const uint32_t *b, size_t nb, uint32_t *out,
+                          size_t out_cap, uint64_t *len_host,
+                          uint64_t *len_dev_user, unsigned flags) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if ((na && !a) || (nb && !b))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL input with non-zero length");
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const bool mat = out != nullptr;
+  const uint64_t mn = std::min<uint64_t>(na, nb);
+  if (mat && out_cap < mn)
+    return ctx_fail(ctx, SETOPS_ERR_CAPACITY,
+                    "out_cap " + std::to_string(out_cap) + " < min(na, nb) " +
+                        std::to_string(mn));
+  CK(cudaSetDevice(ctx->device));
+  const uint32_t *da = a, *db = b;
+  uint32_t *dout = out;
+  if (host) {
+    if (len_dev_user) return ctx_fail(ctx, SETOPS_ERR_INVALID, "async call with host pointers");
+    if (mn > 0) {
+      RK(ctx_stage_in(ctx, 0, a, na, &da));
+      RK(ctx_stage_in(ctx, 1, b, nb, &db));
+    }
+    if (mat) {
+      RK(buf_reserve(ctx, ctx->out0, std::max<uint64_t>(mn, 1) * 4));
+      dout = static_cast<uint32_t *>(ctx->out0.p);
+    }
+  }
+  uint64_t *len_dev = len_dev_user ? len_dev_user : &ctx->dlen[0];
+  if (mn == 0) {
+    if (len_dev_user) {
+      CK(cudaMemsetAsync(len_dev_user, 0, sizeof(uint64_t), ctx->st));
+      return SETOPS_OK;
+    }
+    *len_host = 0;
+    return SETOPS_OK;
+  }
+  PairJob j;
+  j.a = da;
+  j.b = db;
+  j.na = na;
+  j.nb = nb;
+  j.out = mat ? dout : nullptr;
+  j.out_cap = mat ? out_cap : 0;
+  j.len_dev = len_dev;
+  j.choice = ctx_choose(ctx, na, nb, false, flags);
+  RK(ctx_launch_pair(ctx, j));
+  if (len_dev_user) return SETOPS_OK;
+  uint64_t n = 0;
+  RK(ctx_read_u64(ctx, len_dev, &n));
+  if (host && mat && n > 0) {
+    CK(cudaMemcpyAsync(out, dout, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  *len_host = n;
+  return SETOPS_OK;
+}
+
+int setops_gpu_intersect_count(setops_ctx *ctx, const uint32_t *a, size_t na,
+                               const uint32_t *b, size_t nb, uint64_t *count,
+                               unsigned flags) {
+  if (!count) return ctx_fail(ctx, SETOPS_ERR_INVALID, "count is NULL");
+  return intersect_impl(ctx, a, na, b, nb, nullptr, 0, count, nullptr, flags);
+}
+
+int setops_gpu_intersect(setops_ctx *ctx, const uint32_t *a, size_t na,
+                         const uint32_t *b, size_t nb, uint32_t *out,
+                         size_t out_cap, size_t *out_len, unsigned flags) {
+  if (!out_len || (!out && std::min(na, nb) > 0))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "out / out_len is NULL");
+  uint64_t n = 0;
+  uint32_t dummy = 0;
+  int rc = intersect_impl(ctx, a, na, b, nb, out ? out : &dummy, out_cap, &n,
+                          nullptr, flags);
+  if (rc == SETOPS_OK) *out_len = size_t(n);
+  return rc;
+}
+
+int setops_gpu_intersect_async(setops_ctx *ctx, const uint32_t *a, size_t na,
+                               const uint32_t *b, size_t nb, uint32_t *out,
+                               size_t out_cap, uint64_t *len_dev,
+                               unsigned flags) {
+  if (!len_dev) return ctx_fail(ctx, SETOPS_ERR_INVALID, "len_dev is NULL");
+  if (flags & SETOPS_HOST)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "async call with host pointers");
+  return intersect_impl(ctx, a, na, b, nb, out, out_cap, nullptr, len_dev,
+                        flags);
+}
+
+// ---- 2-set BSR ----
+
+static int bsr_impl(setops_ctx *ctx, const uint32_t *ba, const uint32_t *sa,
+                    size_t na, const uint32_t *bb, const uint32_t *sb,
+                    size_t nb, uint32_t *ob, uint32_t *os, size_t out_cap,
+                    uint64_t *len_host, unsigned flags) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if ((na && (!ba || !sa)) || (nb && (!bb || !sb)))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL input with non-zero length");
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const bool mat = ob != nullptr;
+  const uint64_t mn = std::min<uint64_t>(na, nb);
+  if (mat && out_cap < mn)
+    return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap < min(na, nb)");
+  if (mn == 0) {
+    *len_host = 0;
+    return SETOPS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const uint32_t *dba = ba, *dsa = sa, *dbb = bb, *dsb = sb;
+  uint32_t *dob = ob, *dos = os;
+  if (host) {
+    RK(ctx_stage_in(ctx, 0, ba, na, &dba));
+    RK(ctx_stage_in(ctx, 1, bb, nb, &dbb));
+    RK(ctx_stage_in(ctx, 2, sa, na, &dsa));
+    RK(ctx_stage_in(ctx, 3, sb, nb, &dsb));
+    if (mat) {
+      RK(buf_reserve(ctx, ctx->out0, mn * 4));
+      RK(buf_reserve(ctx, ctx->out1, mn * 4));
+      dob = static_cast<uint32_t *>(ctx->out0.p);
+      dos = static_cast<uint32_t *>(ctx->out1.p);
+    }
+  }
+  PairJob j;
+  j.a = dba;
+  j.b = dbb;
+  j.sa = dsa;
+  j.sb = dsb;
+  j.na = na;
+  j.nb = nb;
+  j.bsr = true;
+  j.out = mat ? dob : nullptr;
+  j.out_s = mat ? dos : nullptr;
+  j.out_cap = mat ? out_cap : 0;
+  j.len_dev = &ctx->dlen[0];
+  j.choice = ctx_choose(ctx, na, nb, true, flags);
+  RK(ctx_launch_pair(ctx, j));
+  uint64_t n = 0;
+  RK(ctx_read_u64(ctx, j.len_dev, &n));
+  if (host && mat && n > 0) {
+    CK(cudaMemcpyAsync(ob, dob, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(os, dos, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  *len_host = n;
+  return SETOPS_OK;
+}
+
+int setops_gpu_intersect_bsr_count(setops_ctx *ctx, const uint32_t *bases_a,
+                                   const uint32_t *states_a, size_t na,
+                                   const uint32_t *bases_b,
+                                   const uint32_t *states_b, size_t nb,
+                                   uint64_t *count, unsigned flags) {
+  if (!count) return ctx_fail(ctx, SETOPS_ERR_INVALID, "count is NULL");
+  return bsr_impl(ctx, bases_a, states_a, na, bases_b, states_b, nb, nullptr,
+                  nullptr, 0, count, flags);
+}
+
+int setops_gpu_intersect_bsr(setops_ctx *ctx, const uint32_t *bases_a,
+                             const uint32_t *states_a, size_t na,
+                             const uint32_t *bases_b, const uint32_t *states_b,
+                             size_t nb, uint32_t *out_bases,
+                             uint32_t *out_states, size_t out_cap,
+                             size_t *out_len, unsigned flags) {
+  if (!out_len) return ctx_fail(ctx, SETOPS_ERR_INVALID, "out_len is NULL");
+  if (std::min(na, nb) > 0 && (!out_bases || !out_states))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "output arrays are NULL");
+  uint32_t dummy[2];
+  uint64_t n = 0;
+  int rc = bsr_impl(ctx, bases_a, states_a, na, bases_b, states_b, nb,
+                    out_bases ? out_bases : &dummy[0],
+                    out_states ? out_states : &dummy[1], out_cap, &n, flags);
+  if (rc == SETOPS_OK) *out_len = size_t(n);
+  return rc;
+}
+
+int setops_gpu_bsr_from_sorted(setops_ctx *ctx, const uint32_t *in, size_t n,
+                               uint32_t *bases, uint32_t *states,
+                               size_t *nwords, unsigned flags) {
+  if (!ctx || !nwords || (n && (!in || !bases || !states)))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL argument");
+  if (n == 0) {
+    *nwords = 0;
+    return SETOPS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const uint32_t *din = in;
+  uint32_t *dbs = bases, *dst = states;
+  if (host) {
+    RK(ctx_stage_in(ctx, 0, in, n, &din));
+    RK(buf_reserve(ctx, ctx->out0, n * 4));
+    RK(buf_reserve(ctx, ctx->out1, n * 4));
+    dbs = static_cast<uint32_t *>(ctx->out0.p);
+    dst = static_cast<uint32_t *>(ctx->out1.p);
+  }
+  const uint64_t ntiles = (n + kBsrEncodeTile - 1) / kBsrEncodeTile;
+  int occ = 1;
+  RK(ctx_occupancy(ctx, KernelInfo{bsr_encode_fn(), kUtilThreads, 0, kBsrEncodeTile, "bsr_encode"}, &occ));
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(occ) * ctx->sms));
+  RK(ctx_status_words(ctx, ntiles));
+  uint32_t epoch;
+  RK(ctx_next_epoch(ctx, &epoch));
+  CK(launch_bsr_encode(din, n, dbs, dst, &ctx->dlen[0],
+                       static_cast<uint64_t *>(ctx->status.p), ctx->sync,
+                       ctx->derr, epoch, int(grid), ctx->st));
+  ctx->launches++;
+  uint64_t w = 0;
+  RK(ctx_read_u64(ctx, &ctx->dlen[0], &w));
+  if (host && w) {
+    CK(cudaMemcpyAsync(bases, dbs, w * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(states, dst, w * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  *nwords = size_t(w);
+  return SETOPS_OK;
+}
+
+int setops_gpu_bsr_to_sorted(setops_ctx *ctx, const uint32_t *bases,
+                             const uint32_t *states, size_t n, uint32_t *out,
+                             size_t out_cap, size_t *out_len, unsigned flags) {
+  if (!ctx || !out_len || (n && (!bases || !states || !out)))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL argument");
+  if (n == 0) {
+    *out_len = 0;
+    return SETOPS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const uint32_t *dbs = bases, *dst = states;
+  uint32_t *dout = out;
+  if (host) {
+    RK(ctx_stage_in(ctx, 0, bases, n, &dbs));
+    RK(ctx_stage_in(ctx, 1, states, n, &dst));
+    RK(buf_reserve(ctx, ctx->out0, std::max<size_t>(out_cap, 1) * 4));
+    dout = static_cast<uint32_t *>(ctx->out0.p);
+  }
+  const uint64_t ntiles = (n + kBsrDecodeTile - 1) / kBsrDecodeTile;
+  int occ = 1;
+  RK(ctx_occupancy(ctx, KernelInfo{bsr_decode_fn(), kUtilThreads, 0, kBsrDecodeTile, "bsr_decode"}, &occ));
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(occ) * ctx->sms));
+  RK(ctx_status_words(ctx, ntiles));
+  uint32_t epoch;
+  RK(ctx_next_epoch(ctx, &epoch));
+  CK(launch_bsr_decode(dbs, dst, n, dout, out_cap, &ctx->dlen[0],
+                       static_cast<uint64_t *>(ctx->status.p), ctx->sync,
+                       ctx->derr, epoch, int(grid), ctx->st));
+  ctx->launches++;
+  uint64_t m = 0;
+  RK(ctx_read_u64(ctx, &ctx->dlen[0], &m));
+  if (host && m) {
+    CK(cudaMemcpyAsync(out, dout, m * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  *out_len = size_t(m);
+  return SETOPS_OK;
+}
+
+// ---- k-set SvS ----
+
+static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
+                    const size_t *lens, size_t k, uint32_t *out,
+                    size_t out_cap, uint64_t *len_host, unsigned flags) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if (!sets || !lens || k < 2)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "svs needs k >= 2 sets");
+  for (size_t i = 0; i < k; ++i)
+    if (lens[i] && !sets[i])
+      return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL set with non-zero length");
+  if (k > kLenWords - 2)
+    return ctx_fail(ctx, SETOPS_ERR_TOO_LARGE,
+                    "svs supports up to " + std::to_string(kLenWords - 2) + " sets");
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const bool mat = out != nullptr;
+  std::vector<size_t> order(k);
+  std::iota(order.begin(), order.end(), size_t(0));
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return lens[x] < lens[y]; });
+  const uint64_t mn = lens[order[0]];
+  if (mat && out_cap < mn)
+    return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap < smallest set");
+  if (mn == 0) {
+    *len_host = 0;
+    return SETOPS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  std::vector<const uint32_t *> d(k);
+  if (host) {
+    size_t total = 0;
+    for (size_t i = 0; i < k; ++i) total += lens[i];
+    RK(buf_reserve(ctx, ctx->in[4], total * 4));
+    size_t off = 0;
+    for (size_t i = 0; i < k; ++i) {
+      uint32_t *dst = static_cast<uint32_t *>(ctx->in[4].p) + off;
+      if (lens[i])
+        CK(cudaMemcpyAsync(dst, sets[i], lens[i] * 4, cudaMemcpyHostToDevice,
+                           ctx->st));
+      d[i] = dst;
+      off += lens[i];
+    }
+  } else {
+    for (size_t i = 0; i < k; ++i) d[i] = sets[i];
+  }
+  uint32_t *final_out = out;
+  if (host && mat) {
+    RK(buf_reserve(ctx, ctx->out0, mn * 4));
+    final_out = static_cast<uint32_t *>(ctx->out0.p);
+  }
+  RK(buf_reserve(ctx, ctx->inter[0], mn * 4));
+  RK(buf_reserve(ctx, ctx->inter[1], mn * 4));
+  uint32_t *inter[2] = {static_cast<uint32_t *>(ctx->inter[0].p),
+                        static_cast<uint32_t *>(ctx->inter[1].p)};
+  uint64_t *lens_dev = &ctx->dlen[2];
+  const uint32_t thr = ctx_search_threshold(ctx, false);
+  // step 0: the two smallest sets (lengths known on the host)
+  uint64_t ub = mn;
+  {
+    PairJob j;
+    j.a = d[order[0]];
+    j.na = lens[order[0]];
+    j.b = d[order[1]];
+    j.nb = lens[order[1]];
+    const bool last = (k == 2);
+    j.out = last ? (mat ? final_out : nullptr) : inter[0];
+    j.out_cap = last ? (mat ? out_cap : 0) : mn;
+    j.len_dev = &lens_dev[0];
+    j.choice = ctx_choose(ctx, j.na, j.nb, false, flags);
+    RK(ctx_launch_pair(ctx, j));
+  }
+  for (size_t s = 1; s + 1 < k; ++s) {
+    const bool last = (s + 2 == k);
+    const uint64_t nb = lens[order[s + 1]];
+    PairJob j;
+    j.a = inter[(s - 1) & 1];
+    j.na = ub;
+    j.na_dev = &lens_dev[s - 1];
+    j.b = d[order[s + 1]];
+    j.nb = nb;
+    j.out = last ? (mat ? final_out : nullptr) : inter[s & 1];
+    j.out_cap = last ? (mat ? out_cap : 0) : mn;
+    j.len_dev = &lens_dev[s];
+    if ((flags & SETOPS_ALGO_MASK) != SETOPS_ALGO_AUTO) {
+      j.choice = ctx_choose(ctx, ub, nb, false, flags);
+      RK(ctx_launch_pair(ctx, j));
+    } else {
+      // The intermediate length is only known on the device: launch both
+      // kernels; each checks the actual length ratio and only one runs.
+      j.ratio_thr = thr;
+      j.skip_rule = 2;
+      j.choice.algo = ALGO_MERGE;
+      j.choice.variant = int((ctx->policy[0][0] & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+      RK(ctx_launch_pair(ctx, j));
+      j.skip_rule = 1;
+      j.choice.algo = ALGO_GALLOP;
+      int band = 0;
+      while (band < kRatioBands - 1 && (1u << band) < thr) ++band;
+      j.choice.variant = int((ctx->policy[0][band] & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+      if ((ctx->policy[0][band] & SETOPS_ALGO_MASK) != SETOPS_ALGO_GALLOP) j.choice.variant = 0;
+      RK(ctx_launch_pair(ctx, j));
+    }
+    ub = std::min(ub, nb);
+  }
+  uint64_t n = 0;
+  RK(ctx_read_u64(ctx, &lens_dev[k - 2], &n));
+  if (host && mat && n > 0) {
+    CK(cudaMemcpyAsync(out, final_out, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  *len_host = n;
+  return SETOPS_OK;
+}
+
+int setops_gpu_svs(setops_ctx *ctx, const uint32_t *const *sets,
+                   const size_t *lens, size_t k, uint32_t *out,
+                   size_t out_cap, size_t *out_len, unsigned flags) {
+  if (!out_len) return ctx_fail(ctx, SETOPS_ERR_INVALID, "out_len is NULL");
+  uint32_t dummy = 0;
+  uint64_t n = 0;
+  int rc = svs_impl(ctx, sets, lens, k, out ? out : &dummy, out ? out_cap : 0,
+                    &n, flags);
+  if (rc == SETOPS_OK) *out_len = size_t(n);
+  return rc;
+}
+
+int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
+                         const size_t *lens, size_t k, uint64_t *count,
+                         unsigned flags) {
+  if (!count) return ctx_fail(ctx, SETOPS_ERR_INVALID, "count is NULL");
+  return svs_impl(ctx, sets, lens, k, nullptr, 0, count, flags);
+}
+
+int setops_gpu_validate_sorted(setops_ctx *ctx, const uint32_t *a, size_t n,
+                               int *is_sorted, unsigned flags) {
+  if (!ctx || !is_sorted || (n && !a))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL argument");
+  if (n < 2) {
+    *is_sorted = 1;
+    return SETOPS_OK;
+  }
+  CK(cudaSetDevice(ctx->device));
+  const uint32_t *da = a;
+  if (flags & SETOPS_HOST) RK(ctx_stage_in(ctx, 0, a, n, &da));
+  CK(cudaMemsetAsync(ctx->dflag, 0, sizeof(int), ctx->st));
+  CK(launch_validate_sorted(da, n, ctx->dflag, ctx->sms, ctx->st));
+  ctx->launches++;
+  CK(cudaMemcpyAsync(&ctx->hres[1], ctx->dflag, sizeof(int),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  int bad = 0;
+  std::memcpy(&bad, &ctx->hres[1], sizeof(int));
+  *is_sorted = bad ? 0 : 1;
+  return SETOPS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,172 @@
+"""Benchmark-side inputs: seeded synthetic generators and the datafile format.
+
+Python face of include/setops_bench.h.  The generators restate
+benchmark/src/generators.rs of the reference with a seeded PRNG; the
+datafile functions restate benchmark/src/datafile.rs.  Host only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import lib
+
+
+def _cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def gen_twoset(seed: int, density: float, selectivity: float, small_len: int,
+               large_len: int) -> tuple[np.ndarray, np.ndarray]:
+    """gen_twoset (generators.rs:30-68) for explicit lengths."""
+    s = np.empty(max(small_len, 1), np.uint32)
+    l = np.empty(max(large_len, 1), np.uint32)
+    rc = lib.setops_gen_twoset(seed, density, selectivity, small_len, large_len,
+                               s.ctypes.data, l.ctypes.data)
+    if rc != 0:
+        raise ValueError("setops_gen_twoset: bad arguments")
+    return s[:small_len], l[:large_len]
+
+
+def kset_lens(max_len: int, skewness: float, set_count: int) -> list[int]:
+    lens = (C.c_size_t * set_count)()
+    if lib.setops_gen_kset_lens(max_len, skewness, set_count, lens) != 0:
+        raise ValueError("setops_gen_kset_lens: bad arguments")
+    return list(lens)
+
+
+def gen_kset(seed: int, density: float, selectivity: float, max_len: int,
+             skewness: float, set_count: int) -> list[np.ndarray]:
+    """gen_kset (generators.rs:112-135): smallest set first."""
+    lens = kset_lens(max_len, skewness, set_count)
+    outs = [np.empty(max(n, 1), np.uint32) for n in lens]
+    ptrs = (C.c_void_p * set_count)(*[o.ctypes.data for o in outs])
+    if lib.setops_gen_kset(seed, density, selectivity, max_len, skewness, set_count, ptrs) != 0:
+        raise ValueError("setops_gen_kset: bad arguments")
+    return [o[:n] for o, n in zip(outs, lens)]
+
+
+def sorted_sample(seed: int, n: int, max_value: int) -> np.ndarray:
+    out = np.empty(max(n, 1), np.uint32)
+    if lib.setops_gen_sorted_sample(seed, n, max_value, out.ctypes.data) != 0:
+        raise ValueError("setops_gen_sorted_sample: bad arguments")
+    return out[:n]
+
+
+@dataclass
+class PairBatch:
+    """Uneven pairs stored in one pool: pair p is
+    pool[a_off[p]:a_off[p]+a_len[p]] and pool[b_off[p]:b_off[p]+b_len[p]]."""
+    pool: np.ndarray
+    a_off: np.ndarray
+    a_len: np.ndarray
+    b_off: np.ndarray
+    b_len: np.ndarray
+
+    def __len__(self) -> int:
+        return int(self.a_len.size)
+
+    def pair(self, p: int) -> tuple[np.ndarray, np.ndarray]:
+        return (self.pool[self.a_off[p]:self.a_off[p] + self.a_len[p]],
+                self.pool[self.b_off[p]:self.b_off[p] + self.b_len[p]])
+
+
+def gen_batch(seed: int, npairs: int, min_len: int = 16, max_len: int = 1 << 16,
+              density: tuple[float, float] = (0.01, 0.5),
+              selectivity: tuple[float, float] = (0.0, 0.5),
+              nthreads: int | None = None) -> PairBatch:
+    """Batched uneven pairs: lengths log-uniform in [min_len, max_len]."""
+    a_len = np.empty(npairs, np.uint64)
+    b_len = np.empty(npairs, np.uint64)
+    if lib.setops_gen_batch_sizes(seed, npairs, min_len, max_len, a_len.ctypes.data,
+                                  b_len.ctypes.data) != 0:
+        raise ValueError("setops_gen_batch_sizes: bad arguments")
+    lens = np.empty(2 * npairs, np.uint64)
+    lens[0::2], lens[1::2] = a_len, b_len
+    offs = np.zeros(2 * npairs, np.uint64)
+    if npairs:
+        offs[1:] = np.cumsum(lens[:-1])
+    a_off, b_off = offs[0::2].copy(), offs[1::2].copy()
+    pool = np.empty(max(int(lens.sum()), 1), np.uint32)
+    if lib.setops_gen_batch_fill(seed ^ 0x5EED, npairs, a_len.ctypes.data, b_len.ctypes.data,
+                                 a_off.ctypes.data, b_off.ctypes.data, density[0], density[1],
+                                 selectivity[0], selectivity[1], pool.ctypes.data,
+                                 nthreads or _cores()) != 0:
+        raise ValueError("setops_gen_batch_fill: bad arguments")
+    return PairBatch(pool, a_off, a_len, b_off, b_len)
+
+
+@dataclass
+class PostingIndex:
+    """Posting lists stored in one pool: list i is pool[offs[i]:offs[i]+lens[i]]."""
+    pool: np.ndarray
+    offs: np.ndarray
+    lens: np.ndarray
+    doc_space: int
+
+    def __len__(self) -> int:
+        return int(self.lens.size)
+
+    def list(self, i: int) -> np.ndarray:
+        return self.pool[self.offs[i]:self.offs[i] + self.lens[i]]
+
+
+def gen_index(seed: int, nlists: int, max_len: int = 1 << 20, s: float = 1.1,
+              doc_space: int = 1 << 26, nthreads: int | None = None) -> PostingIndex:
+    """Rank-size Zipf posting lists: |list r| = clip(max_len / r^s, 1, max_len)."""
+    lens = np.empty(nlists, np.uint64)
+    if lib.setops_gen_index_lens(nlists, max_len, s, lens.ctypes.data) != 0:
+        raise ValueError("setops_gen_index_lens: bad arguments")
+    offs = np.zeros(nlists, np.uint64)
+    if nlists:
+        offs[1:] = np.cumsum(lens[:-1])
+    pool = np.empty(max(int(lens.sum()), 1), np.uint32)
+    if lib.setops_gen_index_fill(seed, nlists, lens.ctypes.data, offs.ctypes.data, doc_space,
+                                 pool.ctypes.data, nthreads or _cores()) != 0:
+        raise ValueError("setops_gen_index_fill: bad arguments")
+    return PostingIndex(pool, offs, lens, doc_space)
+
+
+# ---- datafile (benchmark/src/datafile.rs) ---------------------------------
+
+class DatafileError(ValueError):
+    CODES = {-1: "bad argument", -2: "I/O error", -3: "bad set count",
+             -4: "bad magic", -5: "bad endianness", -6: "too many sets"}
+
+    def __init__(self, code: int):
+        super().__init__(self.CODES.get(code, f"error {code}"))
+        self.code = code
+
+
+def datafile_write(path: str, sets) -> None:
+    arrs = [np.ascontiguousarray(s, dtype=np.uint32) for s in sets]
+    n = len(arrs)
+    ptrs = (C.c_void_p * max(n, 1))(*[a.ctypes.data if a.size else None for a in arrs])
+    lens = np.array([a.size for a in arrs], np.uint64)
+    rc = lib.setops_datafile_write(str(path).encode(), ptrs, lens.ctypes.data if n else None, n)
+    if rc != 0:
+        raise DatafileError(rc)
+
+
+def datafile_read(path: str) -> list[np.ndarray]:
+    cnt = C.c_uint64()
+    rc = lib.setops_datafile_read_header(str(path).encode(), C.byref(cnt), None, 0)
+    if rc != 0:
+        raise DatafileError(rc)
+    lens = np.empty(cnt.value, np.uint64)
+    rc = lib.setops_datafile_read_header(str(path).encode(), C.byref(cnt), lens.ctypes.data,
+                                         lens.size)
+    if rc != 0:
+        raise DatafileError(rc)
+    outs = [np.empty(max(int(n), 1), np.uint32) for n in lens]
+    ptrs = (C.c_void_p * len(outs))(*[o.ctypes.data for o in outs])
+    rc = lib.setops_datafile_read_sets(str(path).encode(), ptrs)
+    if rc != 0:
+        raise DatafileError(rc)
+    return [o[:int(n)] for o, n in zip(outs, lens)]

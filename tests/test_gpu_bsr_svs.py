@@ -1,0 +1,138 @@
+"""GPU BSR intersection (vs branchless_merge_bsr), device BSR encode/decode
+(vs BsrVec::from_sorted / to_sorted_set), and device k-set SvS (vs
+svs_generic with naive_merge) -- all bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import pair_with_overlap, rand_set
+
+pytestmark = pytest.mark.gpu
+
+so = pytest.importorskip("simd_set_operations_gb300")
+from simd_set_operations_gb300 import datasets as ds  # noqa: E402
+
+
+def bsr_algos():
+    algos = [so.ALGO_AUTO]
+    algos += [so.ALGO_MERGE | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_MERGE, True))]
+    algos += [so.ALGO_GALLOP | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_GALLOP, True))]
+    return algos
+
+
+def check_bsr(ctx, orc, a, b):
+    ba, sa = orc.bsr_from_sorted(a)
+    bb, sb = orc.bsr_from_sorted(b)
+    wb, ws = orc.branchless_merge_bsr(ba, sa, bb, sb)
+    wc = orc.branchless_merge_bsr_count(ba, sa, bb, sb)
+    assert wc == orc.naive_merge_count(a, b)
+    A, B = so.BsrRef(ba, sa), so.BsrRef(bb, sb)
+    for algo in bsr_algos():
+        v = so.BsrVec()
+        so.gpu_bsr(A, B, v, algo=algo, ctx=ctx)
+        assert np.array_equal(v.bases, wb) and np.array_equal(v.states, ws), hex(algo)
+        c = so.Counter()
+        so.gpu_bsr(A, B, c, algo=algo, ctx=ctx)
+        assert c.count() == wc, hex(algo)
+
+
+def test_bsr_edges(ctx, orc):
+    E = np.empty(0, np.uint32)
+    check_bsr(ctx, orc, E, E)
+    check_bsr(ctx, orc, E, np.arange(100, dtype=np.uint32))
+    x = np.arange(0, 64, dtype=np.uint32)
+    check_bsr(ctx, orc, x, x)
+    check_bsr(ctx, orc, np.arange(0, 64, 2, dtype=np.uint32), np.arange(1, 64, 2, dtype=np.uint32))
+    hi = np.array([2**32 - 33, 2**32 - 32, 2**32 - 2, 2**32 - 1], np.uint32)
+    check_bsr(ctx, orc, hi, hi[1:])
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_bsr_random(ctx, orc, seed):
+    rng = np.random.default_rng(300 + seed)
+    for n, dens in [(100, 0.5), (5000, 0.5), (50_000, 0.3), (200_000, 0.05), (30_000, 0.9)]:
+        span = int(n / dens)
+        a, b = pair_with_overlap(rng, n, int(n * rng.uniform(0.3, 3)), n // 4, hi=span * 3)
+        check_bsr(ctx, orc, a, b)
+
+
+def test_bsr_skewed(ctx, orc):
+    rng = np.random.default_rng(11)
+    s, l = ds.gen_twoset(11, 0.5, 0.1, 2000, 1 << 20)
+    check_bsr(ctx, orc, s, l)
+
+
+@pytest.mark.parametrize("n,hi", [(0, 10), (1, 10), (31, 32), (1000, 2000), (300_000, 400_000),
+                                  (100_000, 1 << 32), (2049, 4096), (70_000, 70_001)])
+def test_bsr_encode_decode(ctx, orc, n, hi):
+    rng = np.random.default_rng(n)
+    s = rand_set(rng, n, hi)
+    wb, ws = orc.bsr_from_sorted(s)
+    v = so.BsrVec.from_sorted(s, ctx=ctx)
+    assert np.array_equal(v.bases, wb) and np.array_equal(v.states, ws)
+    assert np.array_equal(v.to_sorted_set(ctx=ctx), s)
+
+
+def test_run_2set_bsr_property(ctx, orc):
+    """property_tests.rs:82-96: decoded BSR intersection == naive_merge."""
+    rng = np.random.default_rng(12)
+    a, b = pair_with_overlap(rng, 40_000, 50_000, 9000, hi=300_000)
+    A = so.BsrVec.from_sorted(a, ctx=ctx)
+    B = so.BsrVec.from_sorted(b, ctx=ctx)
+    r = so.run_2set_bsr(A.bsr_ref(), B.bsr_ref())
+    assert np.array_equal(r.to_sorted_set(ctx=ctx), orc.naive_merge(a, b))
+
+
+# ---- k-set ----------------------------------------------------------------
+
+def check_svs(ctx, orc, sets):
+    want = orc.svs_generic(sorted(sets, key=len))
+    assert np.array_equal(orc.svs_generic(sets), want)
+    for fn in (so.gpu_auto, so.gpu_merge, so.gpu_galloping):
+        assert np.array_equal(so.run_svs(sets, fn), want), fn
+    assert np.array_equal(so.run_kset(sets, so.gpu_svs), want)
+    c = so.Counter()
+    so.gpu_svs(sets, c)
+    assert c.count() == want.size
+    return want
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5, 8, 12])
+def test_svs_random(ctx, orc, k):
+    rng = np.random.default_rng(400 + k)
+    for trial in range(3):
+        mutual = rand_set(rng, int(rng.integers(0, 2000)), 1 << 22)
+        sets = [np.union1d(rand_set(rng, int(rng.integers(1, 300_000)), 1 << 22), mutual)
+                .astype(np.uint32) for _ in range(k)]
+        check_svs(ctx, orc, sets)
+
+
+def test_svs_edges(ctx, orc):
+    E = np.empty(0, np.uint32)
+    x = np.arange(1000, dtype=np.uint32)
+    check_svs(ctx, orc, [x, x, x])
+    check_svs(ctx, orc, [x, E, x])
+    check_svs(ctx, orc, [x, x[::2], x[::3], x[::5]])
+    check_svs(ctx, orc, [np.arange(0, 10**6, 7, dtype=np.uint32), np.array([7, 14, 999_999], np.uint32)])
+    with pytest.raises(so.SetopsError):
+        so.run_svs([x])
+
+
+@pytest.mark.parametrize("k", [3, 5, 8])
+def test_svs_config_shape(ctx, orc, k):
+    """k-set sets of sizes 2^22 / i, density 0.2, 5% core of the smallest."""
+    sets = ds.gen_kset(500 + k, 0.2, 0.05, 1 << 22, 1.0, k)
+    want = check_svs(ctx, orc, sets)
+    assert want.size >= int(0.05 * sets[0].size)
+
+
+def test_svs_device_pointers(ctx, orc):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    sets = [rand_set(rng, n, 1 << 20) for n in (50_000, 120_000, 300_000, 80_000)]
+    want = orc.svs_generic(sorted(sets, key=len))
+    tsets = [torch.from_numpy(s.view(np.int32)).cuda() for s in sets]
+    w = so.VecWriter()
+    so.gpu_svs(tsets, w, ctx=ctx)
+    assert np.array_equal(w.into(), want)

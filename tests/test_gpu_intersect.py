@@ -1,0 +1,209 @@
+"""GPU 2-set intersection vs the oracle (naive_merge), bit-exact: same
+elements, same ascending order, same count.  Every kernel variant of both
+algorithms is exercised, through host and device pointers."""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, pair_with_overlap, rand_set
+
+pytestmark = pytest.mark.gpu
+
+so = pytest.importorskip("simd_set_operations_gb300")
+from simd_set_operations_gb300 import datasets as ds  # noqa: E402
+
+
+def all_algos():
+    algos = [so.ALGO_AUTO]
+    algos += [so.ALGO_MERGE | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_MERGE))]
+    algos += [so.ALGO_GALLOP | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_GALLOP))]
+    return algos
+
+
+def check_pair(ctx, orc, a, b, algos=None):
+    want = orc.naive_merge(a, b)
+    for algo in (algos or all_algos()):
+        out, n = so.intersect(a, b, algo=algo, ctx=ctx)
+        assert np.array_equal(out[:n], want), (hex(algo), a.size, b.size)
+        assert so.intersect_count(a, b, algo=algo, ctx=ctx) == want.size, hex(algo)
+    return want
+
+
+def test_unit_test_kats(ctx, orc):
+    kat = json.loads((GOLDEN / "unit_tests.json").read_text())
+    for case in kat["twoset"]:
+        a = np.array(case["a"], np.uint32)
+        b = np.array(case["b"], np.uint32)
+        for algo in all_algos():
+            out, n = so.intersect(a, b, algo=algo, ctx=ctx)
+            assert out[:n].tolist() == case["expected"], (case["name"], hex(algo))
+    g = kat["galloping"]
+    large = np.arange(*g["large_range"], dtype=np.uint32)
+    for algo in all_algos():
+        out, n = so.intersect(np.array(g["small"], np.uint32), large, algo=algo, ctx=ctx)
+        assert out[:n].tolist() == g["expected"]
+
+
+def test_reference_kernel_fixtures(ctx, orc):
+    z = np.load(GOLDEN / "ref_kernels.npz")
+    for i in range(len(z["kinds"])):
+        a, b = z[f"a{i}"], z[f"b{i}"]
+        for algo in all_algos():
+            out, n = so.intersect(a, b, algo=algo, ctx=ctx)
+            assert np.array_equal(out[:n], z[f"bmiss{i}"]), (i, hex(algo))
+
+
+def test_edge_cases(ctx, orc):
+    E = np.empty(0, np.uint32)
+    one = np.array([7], np.uint32)
+    rng = np.random.default_rng(1)
+    big = rand_set(rng, 5000)
+    cases = [(E, E), (E, big), (big, E), (one, one), (one, big), (big, big),
+             (np.arange(0, 20000, 2, dtype=np.uint32), np.arange(1, 20000, 2, dtype=np.uint32)),
+             (np.array([0, 2**31 - 1, 2**31, 2**32 - 2, 2**32 - 1], np.uint32),
+              np.array([0, 2**31, 2**32 - 1], np.uint32)),
+             (np.arange(2**32 - 3000, 2**32, dtype=np.uint64).astype(np.uint32),
+              np.arange(2**32 - 6000, 2**32, 3, dtype=np.uint64).astype(np.uint32))]
+    for a, b in cases:
+        check_pair(ctx, orc, a, b)
+
+
+@pytest.mark.parametrize("n", [1, 3, 4, 5, 15, 16, 17, 255, 256, 257, 1023, 1024, 1025,
+                               2047, 2048, 2049, 4095, 4097, 6143, 8193, 16385])
+def test_tile_boundaries(ctx, orc, n):
+    """Sizes around tile (NV = 1024, 2048), ring and 16-byte chunk edges;
+    identical sets put a match on every boundary."""
+    a = np.arange(n, dtype=np.uint32) * 3
+    check_pair(ctx, orc, a, a)
+    b = np.arange(n + 1, dtype=np.uint32) * 3 + 1
+    check_pair(ctx, orc, a, b[: max(n - 1, 0)])
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_pairs(ctx, orc, seed):
+    rng = np.random.default_rng(1000 + seed)
+    for _ in range(6):
+        na = int(rng.integers(0, 200_000))
+        nb = int(rng.integers(0, 200_000))
+        sh = int(rng.integers(0, min(na, nb) + 1))
+        hi = int(rng.choice([max(na + nb, 1) * 2, 1 << 32]))
+        a, b = pair_with_overlap(rng, na, nb, sh, hi)
+        check_pair(ctx, orc, a, b)
+
+
+@pytest.mark.parametrize("ratio", [2, 16, 64, 256, 1024, 16384])
+def test_skewed_pairs(ctx, orc, ratio):
+    rng = np.random.default_rng(ratio)
+    nl = 1 << 20
+    ns = max(nl // ratio, 1)
+    s, l = ds.gen_twoset(ratio, 0.05, 0.1, ns, nl)
+    check_pair(ctx, orc, s, l)
+    check_pair(ctx, orc, l, s)
+
+
+def test_device_pointers_and_misalignment(ctx, orc):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    a, b = pair_with_overlap(rng, 100_003, 77_777, 20_000)
+    want = orc.naive_merge(a, b)
+    for off_a in range(4):
+        for off_b in range(4):
+            ta = torch.zeros(a.size + 4, dtype=torch.int32, device="cuda")
+            tb = torch.zeros(b.size + 4, dtype=torch.int32, device="cuda")
+            ta[off_a:off_a + a.size] = torch.from_numpy(a.view(np.int32))
+            tb[off_b:off_b + b.size] = torch.from_numpy(b.view(np.int32))
+            va, vb = ta[off_a:off_a + a.size], tb[off_b:off_b + b.size]
+            for algo in (so.ALGO_MERGE, so.ALGO_GALLOP, so.ALGO_MERGE | so.VARIANT(2)):
+                out, n = so.intersect(va, vb, algo=algo, ctx=ctx)
+                got = out[:n].cpu().numpy().view(np.uint32)
+                assert np.array_equal(got, want), (off_a, off_b, hex(algo))
+                assert so.intersect_count(va, vb, algo=algo, ctx=ctx) == want.size
+
+
+def test_async_and_capacity(ctx, orc):
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    from simd_set_operations_gb300 import _lib
+    rng = np.random.default_rng(4)
+    a, b = pair_with_overlap(rng, 50_000, 60_000, 1234)
+    ta = torch.from_numpy(a.view(np.int32)).cuda()
+    tb = torch.from_numpy(b.view(np.int32)).cuda()
+    out = torch.empty(50_000, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(2, dtype=torch.int64, device="cuda")
+    rc = _lib.lib.setops_gpu_intersect_async(ctx.handle, ta.data_ptr(), a.size, tb.data_ptr(),
+                                             b.size, out.data_ptr(), 50_000, ln.data_ptr(), 0)
+    assert rc == 0
+    rc = _lib.lib.setops_gpu_intersect_async(ctx.handle, ta.data_ptr(), a.size, tb.data_ptr(),
+                                             b.size, None, 0, ln.data_ptr() + 8, 0)
+    assert rc == 0
+    ctx.synchronize()
+    assert int(ln[0]) == 1234 and int(ln[1]) == 1234
+    assert np.array_equal(out[:1234].cpu().numpy().view(np.uint32), orc.naive_merge(a, b))
+    small = np.empty(10, np.uint32)
+    n = C.c_size_t()
+    rc = _lib.lib.setops_gpu_intersect(ctx.handle, a.ctypes.data, a.size, b.ctypes.data, b.size,
+                                       small.ctypes.data, 10, C.byref(n), _lib.HOST)
+    assert rc == _lib.ERR_CAPACITY
+    # the context is still usable after an error
+    assert so.intersect_count(a, b, ctx=ctx) == 1234
+
+
+def test_many_launches_epoch_wrap(ctx, orc):
+    """More than 2^16 launches on one context: look-back tags wrap."""
+    torch = pytest.importorskip("torch")
+    from simd_set_operations_gb300 import _lib
+    a = np.arange(0, 6000, 3, dtype=np.uint32)
+    b = np.arange(0, 6000, 2, dtype=np.uint32)
+    want = orc.naive_merge(a, b)
+    ta = torch.from_numpy(a.view(np.int32)).cuda()
+    tb = torch.from_numpy(b.view(np.int32)).cuda()
+    out = torch.empty(a.size, dtype=torch.int32, device="cuda")
+    ln = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for i in range(66_000):
+        algo = so.ALGO_MERGE if i % 2 else so.ALGO_GALLOP
+        rc = _lib.lib.setops_gpu_intersect_async(ctx.handle, ta.data_ptr(), a.size,
+                                                 tb.data_ptr(), b.size, out.data_ptr(), a.size,
+                                                 ln.data_ptr(), algo)
+        assert rc == 0
+    ctx.synchronize()
+    assert int(ln[0]) == want.size
+    assert np.array_equal(out[:want.size].cpu().numpy().view(np.uint32), want)
+
+
+def test_full_size_skewed_sweep(ctx, orc):
+    """The 2^24-element sweep: |large| = 2^24, |small| in {2^10, 2^14, 2^18,
+    2^24}, density 0.05, selectivity 0.01; exact vs naive_merge."""
+    for k, e in enumerate((10, 14, 18, 24)):
+        s, l = ds.gen_twoset(100 + k, 0.05, 0.01, 1 << e, 1 << 24)
+        want = orc.naive_merge(s, l)
+        assert want.size == int(0.01 * (1 << e))
+        for algo in (so.ALGO_AUTO, so.ALGO_MERGE, so.ALGO_GALLOP):
+            out, n = so.intersect(s, l, algo=algo, ctx=ctx)
+            assert np.array_equal(out[:n], want), (e, hex(algo))
+
+
+def test_validate_sorted(ctx):
+    assert so.validate_sorted(np.arange(100000, dtype=np.uint32), ctx=ctx)
+    x = np.arange(100000, dtype=np.uint32)
+    x[77777] = x[77776]
+    assert not so.validate_sorted(x, ctx=ctx)
+    assert so.validate_sorted(np.empty(0, np.uint32), ctx=ctx)
+
+
+def test_visitor_api(ctx, orc):
+    rng = np.random.default_rng(8)
+    a, b = pair_with_overlap(rng, 3000, 4000, 500)
+    want = orc.naive_merge(a, b)
+    assert np.array_equal(so.run_2set(a, b, so.gpu_auto), want)
+    assert np.array_equal(so.run_2set(a, b, so.gpu_merge), want)
+    assert np.array_equal(so.run_2set(a, b, so.gpu_galloping), want)
+    assert np.array_equal(so.run_2set_c(a, b, so.gpu_auto_c), want)
+    c = so.Counter()
+    so.gpu_auto(a, b, c)
+    assert c.count() == want.size
+    w = so.UnsafeWriter.with_capacity(min(a.size, b.size))
+    so.gpu_auto(a, b, w)
+    assert np.array_equal(w.into(), want)
