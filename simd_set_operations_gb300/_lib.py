@@ -46,7 +46,7 @@ def _load() -> C.CDLL:
     if not LIB_PATH.exists():
         raise ImportError(
             f"{LIB_PATH} is missing: build it with "
-            "`python -m simd_set_operations_gb300.build` (needs nvcc); "
+            "`python simd_set_operations_gb300/build.py` (needs nvcc); "
             "this package has no CPU fallback")
     return C.CDLL(str(LIB_PATH))
 

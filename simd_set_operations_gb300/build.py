@@ -1,6 +1,6 @@
 """Builds libsetops_gpu.so in-tree for sm_103a (GB300).
 
-    python -m simd_set_operations_gb300.build        # or build() from Python
+    python simd_set_operations_gb300/build.py
 
 Translation units are compiled in parallel into ``_build/`` and linked with
 the static CUDA runtime into ``simd_set_operations_gb300/libsetops_gpu.so``.

@@ -2,9 +2,9 @@
 //
 // * mbarrier + cp.async.bulk (1-D TMA) wrappers for staging input windows in
 //   shared memory (sm_90+ PTX; this library is built for sm_103a only);
-// * bounded spin-waits: every wait has an iteration limit, after which the
-//   kernel records an error code in global memory and returns instead of
-//   hanging the GPU;
+// * bounded spin-waits: every wait has a time limit (GPU global timer),
+//   after which the kernel records an error code in global memory and
+//   returns instead of hanging the GPU;
 // * decoupled look-back over an epoch-tagged status array, used to turn
 //   per-tile match counts into global output offsets in a single pass.
 #pragma once
@@ -22,10 +22,16 @@ enum DeviceError : int {
   DEV_ERR_CAPACITY = 3,          // output would exceed its capacity
 };
 
-// Spin limits.  A try_wait returns after a short hardware time slice, so the
-// mbarrier limit corresponds to well over a second of waiting.
-constexpr uint32_t kMbarSpinLimit = 1u << 24;
-constexpr uint32_t kLookbackSpinLimit = 1u << 26;
+// Wait limits, in nanoseconds of the GPU's global timer.  A bulk copy of a
+// few KB or a predecessor tile publishing its count takes microseconds; a
+// wait that reaches the limit records an error and the kernel returns.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ void record_error(int *err, int code) {
   if (err) atomicCAS(err, 0, code);
@@ -72,8 +78,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // DEV_ERR_TIMEOUT_MBAR) if the limit is reached.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
                                                   uint32_t parity, int *err) {
-  for (uint32_t it = 0; it < kMbarSpinLimit; ++it) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitLimitNs) break;
   }
   record_error(err, DEV_ERR_TIMEOUT_MBAR);
   return false;
@@ -144,13 +153,15 @@ __device__ __forceinline__ uint64_t lookback_exclusive(uint64_t *status,
   st_release_u64(&status[tile], pack_status(epoch, kFlagAggregate, aggregate));
   uint64_t excl = 0;
   int64_t t = int64_t(tile) - 1;
-  uint32_t spins = 0;
+  uint64_t t0 = 0;
   while (t >= 0) {
     uint64_t w = ld_acquire_u64(&status[t]);
     uint32_t e = uint32_t(w >> 48);
     uint64_t flag = (w >> 46) & 3;
     if (e != (epoch & 0xffffu) || flag == 0) {
-      if (++spins > kLookbackSpinLimit) {
+      if (t0 == 0) {
+        t0 = global_ns();
+      } else if (global_ns() - t0 > kWaitLimitNs) {
         record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
         return UINT64_MAX;
       }

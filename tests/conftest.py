@@ -52,6 +52,8 @@ def rand_set(rng, n, hi=1 << 32):
     """Sorted, duplicate-free u32 set of exactly n values below hi."""
     if n == 0:
         return np.empty(0, np.uint32)
+    if n > hi:
+        raise ValueError(f"cannot draw {n} distinct values below {hi}")
     out = np.unique(rng.integers(0, hi, int(n * 1.3) + 16, dtype=np.uint64))
     while out.size < n:
         out = np.unique(np.concatenate([out, rng.integers(0, hi, n, dtype=np.uint64)]))

@@ -52,8 +52,9 @@ def test_bsr_edges(ctx, orc):
 def test_bsr_random(ctx, orc, seed):
     rng = np.random.default_rng(300 + seed)
     for n, dens in [(100, 0.5), (5000, 0.5), (50_000, 0.3), (200_000, 0.05), (30_000, 0.9)]:
-        span = int(n / dens)
-        a, b = pair_with_overlap(rng, n, int(n * rng.uniform(0.3, 3)), n // 4, hi=span * 3)
+        nb = int(n * rng.uniform(0.3, 3))
+        hi = max(int(n / dens) * 3, 2 * (n + nb))
+        a, b = pair_with_overlap(rng, n, nb, n // 4, hi=hi)
         check_bsr(ctx, orc, a, b)
 
 
