@@ -46,7 +46,6 @@ LARGE = 1 << 24
 DENSITY = 0.05
 SELECTIVITY = 0.01
 SEED = 20240601
-HEADLINE = 3  # index of the 2^24 x 2^24 pair
 
 
 def parse():
@@ -58,6 +57,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-sample-seconds", type=float, default=10.0)
+    p.add_argument("--min-warmup-seconds", type=float, default=2.0,
+                   help="keep warming up at least this long (gives the clock sampler "
+                        "load to observe)")
+    p.add_argument("--pairs", default="0,1,2,3",
+                   help="which sweep pairs to run (profiling subsets; default all)")
     return p.parse_args()
 
 
@@ -81,8 +85,8 @@ def algorithmic_bytes(ns: int, nl: int, nout: int) -> int:
     return 4 * (ns + nl) + 4 * nout
 
 
-def workload_config():
-    return {
+def workload_config(sel=None):
+    cfg = {
         "workload": "skewed 2-set sweep: |large| = 2^24, |small| in {2^10, 2^14, 2^18, 2^24}, "
                     "density 0.05, selectivity 0.01, materialised sorted output",
         "pairs_per_step": len(SMALL_EXPS),
@@ -95,6 +99,9 @@ def workload_config():
         "l2": "inputs larger than L2: 321 MiB read per step vs 129 MB L2, each array "
               "touched once per step; no flush",
     }
+    if sel is not None and len(sel) != len(SMALL_EXPS):
+        cfg["pairs_run"] = [1 << SMALL_EXPS[i] for i in sel]
+    return cfg
 
 
 # ---------------------------------------------------------------------------
@@ -308,11 +315,15 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("gloo")
     ctx = so.Context(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream, current for torch too, so that CUDA events and the
+    # library's kernels are ordered on the same stream
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream)
     L = _lib.lib
 
-    pairs = make_sweep(rank)
+    sel = [int(x) for x in args.pairs.split(",")]
+    pairs = [p for i, p in enumerate(make_sweep(rank)) if i in sel]
     dev = []
     for s, l in pairs:
         ds_ = torch.from_numpy(s.view(np.int32)).cuda()
@@ -344,7 +355,7 @@ def run_gb300(args):
     sampler.start()
     t_w = time.perf_counter()
     nw = 0
-    while nw < args.warmup or time.perf_counter() - t_w < 2.0:
+    while nw < args.warmup or time.perf_counter() - t_w < args.min_warmup_seconds:
         step()
         nw += 1
         if nw % 50 == 0:
@@ -387,10 +398,11 @@ def run_gb300(args):
         el_s = float(t.item())
     value = world * len(pairs) * args.steps / el_s
 
-    # roofline: headline merge kernel
-    s_h, l_h = pairs[HEADLINE]
+    # roofline: headline merge kernel (the 2^24 x 2^24 pair)
+    head = max(range(len(pairs)), key=lambda i: pairs[i][0].size)
+    s_h, l_h = pairs[head]
     nout = int(SELECTIVITY * s_h.size)
-    head_ms = statistics.mean(per_pair[HEADLINE])
+    head_ms = statistics.mean(per_pair[head])
     algo_bytes = algorithmic_bytes(s_h.size, l_h.size, nout)
     achieved = algo_bytes / (head_ms / 1e3) / 1e9
     peak, peak_kind = read_peak()
@@ -417,7 +429,6 @@ def run_gb300(args):
             pl = torch.from_numpy(l.view(np.int32)).pin_memory().numpy().view(np.uint32)
             po = torch.empty(s.size, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
             pinned.append((ps, pl, po))
-        ctx.set_stream(None)
         n_out = C.c_size_t()
 
         def step_e2e():
@@ -451,11 +462,10 @@ def run_gb300(args):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "ms_per_step": 1e3 * e_el / e2e_steps,
                "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers"}
-        ctx.set_stream(stream)
 
     # CPU baseline (rank 0 at N=1 only), also the cross-check of the results
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and len(pairs) == len(SMALL_EXPS):
         import oracle
         cores = oracle.host_cores()
         v1, s1, detail, counts, outs, spent = cpu_sweep_best(pairs, 1, args.cpu_sample_seconds)
@@ -478,7 +488,7 @@ def run_gb300(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded; reference generator shape)",
-        "config": workload_config(),
+        "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep,
         "timing": {"bracket_ms_total": wall_ms, "kernel_ms_total": dev_ms,

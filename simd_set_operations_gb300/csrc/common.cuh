@@ -176,6 +176,60 @@ __device__ __forceinline__ uint64_t lookback_exclusive(uint64_t *status,
   return excl;
 }
 
+// Warp-parallel decoupled look-back: call with all 32 lanes of one warp.
+// Each round reads the status words of the 32 preceding tiles at once; the
+// nearest inclusive prefix ends the walk, otherwise the 32 aggregates are
+// added and the window moves back.  Returns the exclusive prefix in every
+// lane (UINT64_MAX on timeout, error recorded).
+__device__ __forceinline__ uint64_t lookback_exclusive_warp(
+    uint64_t *status, uint32_t tile, uint64_t aggregate, uint32_t epoch,
+    int *err) {
+  const int lane = threadIdx.x & 31;
+  if (tile == 0) {
+    if (lane == 0)
+      st_release_u64(&status[0], pack_status(epoch, kFlagPrefix, aggregate));
+    return 0;
+  }
+  if (lane == 0)
+    st_release_u64(&status[tile], pack_status(epoch, kFlagAggregate, aggregate));
+  const uint32_t ep = epoch & 0xffffu;
+  uint64_t excl = 0;
+  int64_t base = int64_t(tile);  // window covers tiles base-1 .. base-32
+  uint64_t t0 = 0;
+  for (;;) {
+    const int64_t idx = base - 1 - lane;
+    uint64_t val = 0;
+    uint32_t flag = uint32_t(kFlagPrefix);  // before tile 0: prefix 0
+    if (idx >= 0) {
+      const uint64_t w = ld_acquire_u64(&status[idx]);
+      flag = (uint32_t(w >> 48) == ep) ? uint32_t((w >> 46) & 3) : 0u;
+      val = w & kValueMask;
+    }
+    const unsigned pre = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+    const unsigned nrd = __ballot_sync(0xffffffffu, flag == 0);
+    const int p = pre ? __ffs(pre) - 1 : 32;
+    const unsigned need = (p >= 31) ? 0xffffffffu : ((2u << p) - 1u);
+    if (nrd & need) {
+      if (t0 == 0) {
+        t0 = global_ns();
+      } else if (global_ns() - t0 > kWaitLimitNs) {
+        if (lane == 0) record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
+        return UINT64_MAX;
+      }
+      continue;
+    }
+    uint64_t c = (lane <= p) ? val : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    excl += c;
+    if (p < 32) break;
+    base -= 32;
+  }
+  if (lane == 0)
+    st_release_u64(&status[tile], pack_status(epoch, kFlagPrefix, excl + aggregate));
+  return excl;
+}
+
 // True when a kernel with device-side choice rule `rule` should not run for
 // lengths (na, nb): rule 1 runs only when max/min >= thr, rule 2 only below.
 // An empty input counts as "search" (either kernel returns 0).

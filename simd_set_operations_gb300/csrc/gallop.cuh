@@ -5,20 +5,24 @@
 // the smaller set is looked up in the larger one; the output is the matching
 // elements of the small set in their (ascending) order.
 //
-// GPU form: the exponential phase of galloping exists to find a bracket
-// cheaply from the previous position.  On the GPU all small elements are
-// searched at once, so the bracket comes from a shared-memory sample of the
-// large set instead (NSAMP block maxima, loaded once per CTA); the search
-// inside the bracket is then either
-//   * GS == 1: one thread per element, a branchless binary search, ITEMS
-//     independent searches interleaved per thread for memory-level
-//     parallelism; or
-//   * GS > 1: GS lanes per element, each round probing GS points of the
-//     bracket at once and narrowing it (GS+1)-fold (warp ballot), so a
-//     2^13-element bracket needs 3 dependent rounds with GS = 32.
-// Output order is preserved by tiles (TILE consecutive small elements)
-// claimed in order from an atomic ticket and combined with decoupled
-// look-back.
+// GPU form.  Galloping's exponential phase exists to find a bracket cheaply
+// from the previous position; on the GPU all small elements are searched at
+// once, so brackets come from cooperative searches instead:
+//   * each CTA owns a contiguous run of small elements (one static range per
+//     CTA, like the merge kernel's diagonal ranges);
+//   * NSAMP > 0: the CTA finds the large-set bracket of its whole run with
+//     two (NT+1)-ary block searches, then loads a shared-memory sample of NSAMP
+//     bracket maxima, so each element starts from a narrow block;
+//     NSAMP == 0: every element searches the whole large set (no per-CTA
+//     preparation; best when a CTA has few elements);
+//   * the search inside the block is either GS == 1: one thread per element,
+//     branchless binary search, ITEMS interleaved per thread for memory-level
+//     parallelism; or GS > 1: GS lanes per element probing GS points per
+//     round ((GS+1)-ary narrowing via warp ballot).
+// Matches are staged per CTA (block scan per pass, order preserved) in a
+// scratch region at the CTA's first element (a CTA cannot emit more matches
+// than elements it owns); one warp-parallel look-back per CTA gives its
+// output offset.
 #pragma once
 
 #include "common.cuh"
@@ -33,11 +37,13 @@ struct GallopArgs {
   uint64_t na, nb;
   const uint64_t *na_dev;
   const uint64_t *nb_dev;
+  uint32_t *stage;    // scratch, >= min(na, nb) words (materialise)
+  uint32_t *stage_s;  // scratch states (BSR materialise)
   uint32_t *out;
   uint32_t *out_s;
   uint64_t out_cap;
   uint64_t *out_len;  // elements (count / array) or words (BSR materialise)
-  uint64_t *status;   // look-back words, >= number of tiles
+  uint64_t *status;   // look-back words, >= gridDim.x entries
   LaunchSync *sync;
   int *err;
   uint32_t epoch;
@@ -53,8 +59,9 @@ struct GallopCfg {
   static_assert(GS == 1 || GS == 2 || GS == 4 || GS == 8 || GS == 16 ||
                     GS == 32,
                 "group size must divide a warp");
+  static_assert(GS == 1 || ITEMS == 1, "groups search one element at a time");
   static constexpr int kNG = NT / GS;
-  static constexpr int kTile = kNG * ITEMS;
+  static constexpr int kTile = kNG * ITEMS;  // elements per pass of a CTA
 };
 
 // First index k in samp[0..n) with samp[k] >= x (n if none).
@@ -73,19 +80,45 @@ __device__ __forceinline__ uint32_t smem_lower_bound(const uint32_t *samp,
   return lo;
 }
 
+// CTA-cooperative lower_bound: first index in [lo, hi) with L[i] >= x (hi
+// if none).  Each round all NT threads probe evenly spaced points and the
+// bracket narrows (NT+1)-fold (3 rounds for 2^24 elements at NT = 256).
+// Call from every thread of the block with the same arguments.
+template <int NT>
+__device__ __forceinline__ uint64_t block_lower_bound(const uint32_t *L,
+                                                      uint64_t lo, uint64_t hi,
+                                                      uint32_t x) {
+  const int t = threadIdx.x;
+  while (hi > lo) {
+    const uint64_t span = hi - lo;
+    if (span <= uint64_t(NT)) {
+      const bool pr = uint64_t(t) < span && __ldg(L + lo + t) < x;
+      lo += uint64_t(__syncthreads_count(pr));
+      break;
+    }
+    const uint64_t xp = lo + (uint64_t(t + 1) * span) / (NT + 1);
+    const uint64_t c = uint64_t(__syncthreads_count(__ldg(L + xp) < x));
+    const uint64_t nhi = (c < uint64_t(NT)) ? lo + ((c + 1) * span) / (NT + 1) : hi;
+    if (c > 0) lo = lo + (c * span) / (NT + 1) + 1;
+    hi = nhi;
+  }
+  return lo;
+}
+
 template <int NT, int GS, int ITEMS, int NSAMP, bool BSR, bool MAT>
 __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
   using Cfg = GallopCfg<NT, GS, ITEMS, NSAMP>;
   constexpr int TILE = Cfg::kTile;
-  constexpr int PT = (TILE + NT - 1) / NT;  // compaction positions / thread
+  constexpr int SAMP = NSAMP > 0 ? NSAMP : 1;
 
-  __shared__ uint32_t samp[NSAMP];
+  __shared__ uint32_t samp[SAMP];
   __shared__ uint32_t sHit[TILE];
   __shared__ uint32_t sKey[MAT ? TILE : 1];
   __shared__ uint32_t sSt[(MAT && BSR) ? TILE : 1];
   __shared__ uint32_t warp_sums[NT / 32];
-  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_vid;
   __shared__ unsigned long long s_excl;
+  __shared__ unsigned long long red[NT / 32];
 
   const int t = threadIdx.x;
   const int lane = t & 31;
@@ -98,47 +131,69 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
     tp = SS; SS = SL; SL = tp;
     uint64_t tn = ns; ns = nl; nl = tn;
   }
-  const uint64_t ntiles = (ns + TILE - 1) / TILE;
   if (skip_by_rule(p.skip_rule, p.ratio_thr, ns, nl)) return;
 
-  // ---- sample of the large set: block maxima ----
-  const uint64_t st = nl == 0 ? 1 : (nl + NSAMP - 1) / NSAMP;
-  const uint32_t nblk = nl == 0 ? 0 : uint32_t((nl + st - 1) / st);
-  for (uint32_t kb = t; kb < nblk; kb += NT) {
-    uint64_t e = uint64_t(kb + 1) * st;
-    if (e > nl) e = nl;
-    samp[kb] = __ldg(L + e - 1);
-  }
+  if (t == 0) s_vid = atomicAdd(&p.sync->ticket, 1u);
   __syncthreads();
+  const uint32_t vid = s_vid;
+  const uint32_t G = gridDim.x;
+  const uint64_t per = (ns + G - 1) / G;
+  const uint64_t s0 = (uint64_t(vid) * per < ns) ? uint64_t(vid) * per : ns;
+  const uint64_t s1 = (s0 + per < ns) ? s0 + per : ns;
 
-  uint64_t cnt = 0;
-  for (;;) {
-    if (t == 0) s_tile = atomicAdd(&p.sync->ticket, 1u);
+  // ---- bracket of this CTA's run in L, and its sample ----
+  uint64_t blo = 0, bhi = nl;  // candidates for S[s0..s1) lie in L[blo, bhi)
+  uint64_t st = 1;
+  uint32_t nblk = 0;
+  if (NSAMP > 0 && s1 > s0 && nl > 0) {
+    const uint32_t xf = __ldg(S + s0), xl = __ldg(S + s1 - 1);
+    blo = block_lower_bound<NT>(L, 0, nl, xf);
+    const uint64_t lbl = block_lower_bound<NT>(L, blo, nl, xl);
+    bhi = lbl < nl ? lbl + 1 : nl;  // lower_bound of the last is a candidate
+    const uint64_t len = bhi > blo ? bhi - blo : 0;
+    st = len == 0 ? 1 : (len + SAMP - 1) / SAMP;
+    nblk = len == 0 ? 0 : uint32_t((len + st - 1) / st);
+    for (uint32_t kb = t; kb < nblk; kb += NT) {
+      uint64_t e = blo + uint64_t(kb + 1) * st;
+      if (e > bhi) e = bhi;
+      samp[kb] = __ldg(L + e - 1);
+    }
     __syncthreads();
-    const uint32_t tile = s_tile;
-    if (uint64_t(tile) >= ntiles) break;
-    const uint64_t base = uint64_t(tile) * TILE;
+  }
 
+  // Bracket [lo, lo+len) inside which lower_bound(L, x) lies, or len == 0
+  // with lo == nl when x exceeds the candidates.
+  auto bracket = [&](uint32_t x, uint64_t &lo, uint64_t &len) {
+    if (NSAMP > 0) {
+      const uint32_t kb = smem_lower_bound(samp, nblk, x);
+      if (kb >= nblk) {
+        lo = nl;
+        len = 0;
+        return;
+      }
+      lo = blo + uint64_t(kb) * st;
+      const uint64_t e = (lo + st < bhi) ? lo + st : bhi;
+      len = e - lo;
+    } else {
+      lo = 0;
+      len = nl;
+    }
+  };
+
+  uint64_t cnt = 0;      // count mode (BSR: elements)
+  uint64_t cta_cnt = 0;  // materialise: matches staged so far
+  for (uint64_t base = s0; base < s1; base += TILE) {
     if (GS == 1) {
-      // ITEMS interleaved branchless searches per thread
       uint32_t x[ITEMS];
       uint64_t lo[ITEMS], len[ITEMS];
       bool valid[ITEMS];
 #pragma unroll
       for (int it = 0; it < ITEMS; ++it) {
         const uint64_t idx = base + uint64_t(t) * ITEMS + it;
-        valid[it] = idx < ns;
+        valid[it] = idx < s1;
         x[it] = valid[it] ? __ldg(S + idx) : 0u;
-        const uint32_t kb = valid[it] ? smem_lower_bound(samp, nblk, x[it]) : nblk;
-        if (kb >= nblk) {
-          valid[it] = false;
-          lo[it] = 0;
-          len[it] = 0;
-        } else {
-          lo[it] = uint64_t(kb) * st;
-          const uint64_t e = (lo[it] + st < nl) ? lo[it] + st : nl;
-          len[it] = e - lo[it];
-        }
+        if (valid[it]) bracket(x[it], lo[it], len[it]);
+        else { lo[it] = nl; len[it] = 0; }
       }
       bool more = true;
       while (more) {
@@ -173,62 +228,52 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
         }
       }
     } else {
-      // GS lanes per element, (GS+1)-ary narrowing per round
       const int g = t / GS, gl = t & (GS - 1);
-      const unsigned gmask =
-          (GS == 32) ? 0xffffffffu
-                     : (((1u << GS) - 1u) << (lane & ~(GS - 1)));
+      const unsigned gbits = (GS == 32) ? 0xffffffffu : ((1u << GS) - 1u);
       const int gshift = lane & ~(GS - 1);
-      for (int it = 0; it < ITEMS; ++it) {
-        const uint64_t idx = base + uint64_t(g) * ITEMS + it;
-        bool hit = false;
-        uint32_t x = 0, stv = 0;
-        if (idx < ns) {
-          x = __ldg(S + idx);
-          const uint32_t kb = smem_lower_bound(samp, nblk, x);
-          if (kb < nblk) {
-            uint64_t lo = uint64_t(kb) * st;
-            uint64_t hi = (lo + st < nl) ? lo + st : nl;
-            while (hi - lo > uint64_t(GS)) {
-              const uint64_t span = hi - lo;
-              const uint64_t xp = lo + (uint64_t(gl + 1) * span) / (GS + 1);
-              const bool pr = __ldg(L + xp) < x;
-              const uint64_t c =
-                  __popc((__ballot_sync(gmask, pr) >> gshift) &
-                         ((GS == 32) ? 0xffffffffu : ((1u << GS) - 1u)));
-              const uint64_t nhi =
-                  (c < uint64_t(GS)) ? lo + ((c + 1) * span) / (GS + 1) : hi;
-              if (c > 0) lo = lo + (c * span) / (GS + 1) + 1;
-              hi = nhi;
-            }
+      const unsigned gmask = gbits << gshift;
+      const uint64_t idx = base + uint64_t(g);
+      bool hit = false;
+      uint32_t x = 0, stv = 0;
+      if (idx < s1) {
+        x = __ldg(S + idx);
+        uint64_t lo, len;
+        bracket(x, lo, len);
+        if (len > 0) {
+          uint64_t hi = lo + len;
+          while (hi - lo > uint64_t(GS)) {
             const uint64_t span = hi - lo;
-            const bool pr = (uint64_t(gl) < span) && (__ldg(L + lo + gl) < x);
-            const uint64_t c =
-                __popc((__ballot_sync(gmask, pr) >> gshift) &
-                       ((GS == 32) ? 0xffffffffu : ((1u << GS) - 1u)));
-            const uint64_t lb = lo + c;
-            hit = lb < nl && __ldg(L + lb) == x;
-            if (BSR && hit) {
-              stv = __ldg(SS + idx) & __ldg(SL + lb);
-              hit = stv != 0;
-            }
+            const uint64_t xp = lo + (uint64_t(gl + 1) * span) / (GS + 1);
+            const bool pr = __ldg(L + xp) < x;
+            const uint64_t c = __popc((__ballot_sync(gmask, pr) >> gshift) & gbits);
+            const uint64_t nhi = (c < uint64_t(GS)) ? lo + ((c + 1) * span) / (GS + 1) : hi;
+            if (c > 0) lo = lo + (c * span) / (GS + 1) + 1;
+            hi = nhi;
+          }
+          const uint64_t span = hi - lo;
+          const bool pr = (uint64_t(gl) < span) && (__ldg(L + lo + gl) < x);
+          const uint64_t lb = lo + __popc((__ballot_sync(gmask, pr) >> gshift) & gbits);
+          hit = lb < nl && __ldg(L + lb) == x;
+          if (BSR && hit) {
+            stv = __ldg(SS + idx) & __ldg(SL + lb);
+            hit = stv != 0;
           }
         }
-        if (gl == 0) {
-          const int pos = g * ITEMS + it;
-          if (MAT) {
-            sHit[pos] = hit;
-            sKey[pos] = x;
-            if (BSR) sSt[pos] = stv;
-          } else {
-            cnt += BSR ? (hit ? __popc(stv) : 0) : (hit ? 1 : 0);
-          }
+      }
+      if (gl == 0) {
+        if (MAT) {
+          sHit[g] = hit;
+          sKey[g] = x;
+          if (BSR) sSt[g] = stv;
+        } else {
+          cnt += BSR ? (hit ? __popc(stv) : 0) : (hit ? 1 : 0);
         }
       }
     }
 
     if (MAT) {
       __syncthreads();
+      constexpr int PT = (TILE + NT - 1) / NT;  // positions per thread
       uint32_t mine = 0;
 #pragma unroll
       for (int q = 0; q < PT; ++q) {
@@ -237,49 +282,61 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
       }
       uint32_t tot;
       const uint32_t ex = block_exclusive_scan<NT>(mine, warp_sums, &tot);
-      if (t == 0) s_excl = lookback_exclusive(p.status, tile, tot, p.epoch, p.err);
-      __syncthreads();
-      const uint64_t tex = s_excl;
-      if (tex == UINT64_MAX) return;  // error recorded; host resets state
-      if (tex + tot > p.out_cap) {
-        if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
-        return;
-      }
-      uint64_t o = tex + ex;
+      uint64_t o = s0 + cta_cnt + ex;
 #pragma unroll
       for (int q = 0; q < PT; ++q) {
         const int pos = t * PT + q;
         if (pos < TILE && sHit[pos]) {
-          p.out[o] = sKey[pos];
-          if (BSR) p.out_s[o] = sSt[pos];
+          p.stage[o] = sKey[pos];
+          if (BSR) p.stage_s[o] = sSt[pos];
           ++o;
         }
       }
-      if (tile == ntiles - 1 && t == 0) *p.out_len = tex + tot;
+      cta_cnt += tot;
+      __syncthreads();  // sHit / sKey reused by the next pass
     }
-    __syncthreads();  // s_tile / smem tile buffers are reused
   }
 
-  // ---- combine counts, reset coordination words ----
+  // ---- combine ----
   if (!MAT) {
     uint64_t v = cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __shared__ unsigned long long red[NT / 32];
     if (lane == 0) red[t >> 5] = v;
     __syncthreads();
     if (t == 0) {
       unsigned long long s = 0;
       for (int w = 0; w < NT / 32; ++w) s += red[w];
       if (s) atomicAdd(&p.sync->acc, s);
+      __threadfence();
+      if (atomicAdd(&p.sync->done, 1u) == G - 1) {
+        *p.out_len = atomicExch(&p.sync->acc, 0ull);
+        p.sync->ticket = 0;
+        p.sync->done = 0;
+        __threadfence();
+      }
+    }
+    return;
+  }
+  if (t < 32) {
+    const uint64_t ex = lookback_exclusive_warp(p.status, vid, cta_cnt, p.epoch, p.err);
+    if (t == 0) {
+      s_excl = ex;
+      if (ex != UINT64_MAX && ex + cta_cnt > p.out_cap)
+        record_error(p.err, DEV_ERR_CAPACITY);
     }
   }
+  __syncthreads();
+  const uint64_t ex = s_excl;
+  if (ex == UINT64_MAX || ex + cta_cnt > p.out_cap) return;
+  for (uint64_t q = t; q < cta_cnt; q += NT) {
+    p.out[ex + q] = p.stage[s0 + q];
+    if (BSR) p.out_s[ex + q] = p.stage_s[s0 + q];
+  }
   if (t == 0) {
+    if (vid == G - 1) *p.out_len = ex + cta_cnt;
     __threadfence();
-    const uint32_t prev = atomicAdd(&p.sync->done, 1u);
-    if (prev == gridDim.x - 1) {
-      if (!MAT) *p.out_len = atomicExch(&p.sync->acc, 0ull);
-      else if (ntiles == 0) *p.out_len = 0;
+    if (atomicAdd(&p.sync->done, 1u) == G - 1) {
       p.sync->ticket = 0;
       p.sync->done = 0;
       __threadfence();

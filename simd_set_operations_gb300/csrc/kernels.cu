@@ -9,11 +9,11 @@ namespace setops {
 
 namespace {
 
-template <int NT, int VT, int RLOG, bool BSR, bool MAT>
+template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
 KernelInfo mk_merge(const char *name) {
   return KernelInfo{reinterpret_cast<const void *>(
-                        &merge_kernel<NT, VT, RLOG, BSR, MAT>),
-                    NT, MergeCfg<NT, VT, RLOG, BSR, MAT>::kSmemBytes, NT * VT,
+                        &merge_kernel<NT, C, NS, BMW, BSR, MAT>),
+                    NT, MergeCfg<NT, C, NS, BMW, BSR, MAT>::kSmemBytes, C,
                     name};
 }
 
@@ -25,37 +25,43 @@ KernelInfo mk_gallop(const char *name) {
 }
 
 // [variant][count, materialise]
-#define MERGE_ROW(NT, VT, RL, BSR)                                   \
-  {mk_merge<NT, VT, RL, BSR, false>("merge_" #NT "x" #VT "_r" #RL),  \
-   mk_merge<NT, VT, RL, BSR, true>("merge_" #NT "x" #VT "_r" #RL)}
-#define GALLOP_ROW(NT, GS, IT, BSR)                                       \
-  {mk_gallop<NT, GS, IT, 2048, BSR, false>("gallop_" #NT "_g" #GS "_i" #IT), \
-   mk_gallop<NT, GS, IT, 2048, BSR, true>("gallop_" #NT "_g" #GS "_i" #IT)}
+#define MERGE_ROW(NT, C, NS, BM, BSR)                                          \
+  {mk_merge<NT, C, NS, BM, BSR, false>("merge_" #NT "_c" #C "x" #NS "_t" #BM), \
+   mk_merge<NT, C, NS, BM, BSR, true>("merge_" #NT "_c" #C "x" #NS "_t" #BM)}
+#define GALLOP_ROW(NT, GS, IT, NS, BSR)                                         \
+  {mk_gallop<NT, GS, IT, NS, BSR, false>("gallop_" #NT "_g" #GS "_i" #IT "_s" #NS), \
+   mk_gallop<NT, GS, IT, NS, BSR, true>("gallop_" #NT "_g" #GS "_i" #IT "_s" #NS)}
 
+// NT threads; NS slots of C-element chunks per input; window tables of BM
+// words per set (bitmaps of 32*BM values, or BM BSR states)
 const KernelInfo kMergeU32[][2] = {
-    MERGE_ROW(256, 8, 13, false),   // 0: NV 2048, 64 KB rings
-    MERGE_ROW(128, 16, 13, false),  // 1: NV 2048, fewer threads, longer runs
-    MERGE_ROW(256, 4, 12, false),   // 2: NV 1024, 32 KB rings
-    MERGE_ROW(512, 4, 13, false),   // 3: NV 2048, 16 warps
-    MERGE_ROW(128, 8, 12, false),   // 4: NV 1024, 4 warps
+    MERGE_ROW(256, 2048, 3, 2048, false),  // 0: 64 KB, 3 CTAs/SM
+    MERGE_ROW(256, 2048, 4, 2048, false),  // 1: 80 KB, deeper prefetch
+    MERGE_ROW(256, 1024, 4, 2048, false),  // 2: 48 KB, 4 CTAs/SM
+    MERGE_ROW(512, 2048, 3, 4096, false),  // 3: wide windows, 16 warps
+    MERGE_ROW(256, 4096, 2, 2048, false),  // 4: big chunks
+    MERGE_ROW(128, 1024, 4, 1024, false),  // 5: 40 KB, 4 warps
 };
 const KernelInfo kMergeBsr[][2] = {
-    MERGE_ROW(128, 8, 12, true),   // 0: NV 1024, 64 KB rings
-    MERGE_ROW(256, 4, 12, true),   // 1
-    MERGE_ROW(256, 8, 13, true),   // 2: NV 2048, 128 KB rings
+    MERGE_ROW(256, 1024, 3, 2048, true),  // 0: 64 KB
+    MERGE_ROW(256, 2048, 2, 2048, true),  // 1: 80 KB
+    MERGE_ROW(128, 1024, 3, 1024, true),  // 2: 56 KB
 };
+// GS lanes per element (1 = thread per element with IT interleaved
+// searches); NS = shared-memory sample of the CTA's bracket (0 = none)
 const KernelInfo kGallopU32[][2] = {
-    GALLOP_ROW(256, 1, 4, false),   // 0: thread per element, 4 interleaved
-    GALLOP_ROW(256, 4, 2, false),   // 1
-    GALLOP_ROW(256, 8, 1, false),   // 2
-    GALLOP_ROW(256, 32, 1, false),  // 3: warp per element
-    GALLOP_ROW(128, 32, 1, false),  // 4
-    GALLOP_ROW(256, 1, 1, false),   // 5
+    GALLOP_ROW(256, 1, 4, 2048, false),  // 0: sampled, thread per element
+    GALLOP_ROW(256, 16, 1, 0, false),    // 1: 17-ary over the whole set
+    GALLOP_ROW(256, 32, 1, 0, false),    // 2: warp per element, 33-ary
+    GALLOP_ROW(256, 8, 1, 0, false),     // 3: 9-ary, 4 elements per warp
+    GALLOP_ROW(256, 1, 8, 2048, false),  // 4: sampled, 8 interleaved
+    GALLOP_ROW(256, 32, 1, 2048, false), // 5: sampled, warp per element
+    GALLOP_ROW(256, 8, 1, 2048, false),  // 6: sampled, 9-ary
 };
 const KernelInfo kGallopBsr[][2] = {
-    GALLOP_ROW(256, 1, 4, true),
-    GALLOP_ROW(256, 8, 1, true),
-    GALLOP_ROW(256, 32, 1, true),
+    GALLOP_ROW(256, 1, 4, 2048, true),
+    GALLOP_ROW(256, 16, 1, 0, true),
+    GALLOP_ROW(256, 32, 1, 0, true),
 };
 
 template <class T, size_t N>
@@ -145,7 +151,10 @@ __global__ void __launch_bounds__(kUtilThreads)
       starts += (i == 0) || ((__ldg(in + i) >> 5) != (__ldg(in + i - 1) >> 5));
     uint32_t tot;
     const uint32_t ex = block_exclusive_scan<NT>(starts, warp_sums, &tot);
-    if (t == 0) s_excl = lookback_exclusive(status, tile, tot, epoch, err);
+    if (t < 32) {
+      const uint64_t lx = lookback_exclusive_warp(status, tile, tot, epoch, err);
+      if (t == 0) s_excl = lx;
+    }
     __syncthreads();
     const uint64_t tex = s_excl;
     if (tex == UINT64_MAX) return;
@@ -203,7 +212,10 @@ __global__ void __launch_bounds__(kUtilThreads)
       if (w0 + q < n) mine += __popc(__ldg(states + w0 + q));
     uint32_t tot;
     const uint32_t ex = block_exclusive_scan<NT>(mine, warp_sums, &tot);
-    if (t == 0) s_excl = lookback_exclusive(status, tile, tot, epoch, err);
+    if (t < 32) {
+      const uint64_t lx = lookback_exclusive_warp(status, tile, tot, epoch, err);
+      if (t == 0) s_excl = lx;
+    }
     __syncthreads();
     const uint64_t tex = s_excl;
     if (tex == UINT64_MAX) return;

@@ -4,31 +4,37 @@
 // Semantics follow the reference's naive_merge (setops/src/intersect/
 // merge.rs:7-33) and branchless_merge_bsr (merge.rs:62-87): the output is the
 // ascending intersection, with the Counter visitor's count
-// (setops/src/visitor.rs:24-49, BSR: sum of popcount(state), visitor.rs:399).
+// (setops/src/visitor.rs:24-49; BSR: sum of popcount(state), visitor.rs:399).
 //
-// Layout of the work
-// ------------------
-// Let A be the smaller input.  Merge the two arrays conceptually, taking A
-// first on ties; a match is then an A element whose successor in the merge is
-// an equal B element.  The merged sequence (length na+nb) is cut into one
-// contiguous diagonal range per CTA.  A CTA
-//   1. finds the merge-path co-rank of its first diagonal with a cooperative
-//      (NT+1)-ary search over global memory (3 rounds for 2^24 elements);
-//   2. streams its range in tiles of NV = NT*VT merged elements.  Both inputs
-//      are staged in shared-memory rings (R words each) by 1-D bulk copies
-//      (cp.async.bulk, completing on one of two mbarriers), issued two tiles
-//      ahead of use;
-//   3. per tile, every thread binary-searches its own sub-diagonal in the
-//      rings and walks VT merge steps, counting (or staging) matches;
-//   4. count mode: one atomic add per CTA, the last CTA to finish writes the
-//      total.  Materialise mode: matches go to a scratch stage at the CTA's
-//      A co-rank (an exclusive region: a CTA can never emit more matches than
-//      A elements it consumes), then decoupled look-back over CTAs gives each
-//      CTA its output offset and it copies its run to the output.
+// Work layout
+// -----------
+// Let A be the smaller input.  The merged sequence (A first on ties; length
+// na+nb) is cut into one contiguous diagonal range per CTA, whose merge-path
+// co-ranks (both ends) one block search finds.  The CTA owns A[ia0, ia1) and
+// reads B[ib0, ib1] -- B[ib1] is the one element past the range that can
+// equal the CTA's last A element; a match is counted by the CTA owning its A
+// element, so every match is counted once.
 //
-// A match whose A element is the last one a thread/tile/CTA consumes looks
-// one element ahead into B; the rings always hold B up to one element past
-// the tile window, so no match is lost or counted twice at any boundary.
+// The two runs stream independently through shared memory: fixed chunks of
+// C elements, 16-byte aligned, loaded by 1-D TMA bulk copies into NS slots
+// per stream, each slot with its own mbarrier; a slot is refilled as soon as
+// its chunk is used up.
+//
+// Dense runs (at least one element per 64 values) are intersected in value
+// windows: every element of window [w, w + 32*BMW) sets its bit in its
+// set's window bitmap (atomicOr; for BSR the state word is stored at its
+// base), the two tables are AND-ed word by word, and the set bits are the
+// matches, already in ascending order (one block scan per window orders the
+// output).  The next window starts at the smallest value not yet consumed,
+// so empty value ranges are skipped.  Sparse runs are intersected chunk pair
+// by chunk pair (binary search of each A element in the B chunk, advancing
+// the chunk with the smaller maximum, as in the reference's block-wise SIMD
+// algorithms, setops/src/intersect/shuffling.rs:69-112).
+//
+// Count mode adds per-CTA totals atomically; the last CTA writes the total.
+// Materialise mode stages a CTA's matches in scratch at its first A index
+// (an exclusive region: a CTA cannot emit more matches than A elements it
+// owns); decoupled look-back over CTAs gives each CTA its output offset.
 #pragma once
 
 #include "common.cuh"
@@ -61,116 +67,208 @@ struct MergeArgs {
   uint32_t ratio_thr;
 };
 
-template <int NT, int VT, int RLOG, bool BSR, bool MAT>
+// Shapes: NT threads, chunks of C elements per stream, NS chunk slots per
+// stream, window tables of BMW words per set.
+template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
 struct MergeCfg {
-  static constexpr int kNT = NT;
-  static constexpr int kVT = VT;
-  static constexpr int kNV = NT * VT;
-  static constexpr uint32_t kR = 1u << RLOG;
-  // Prefetch frontier is two tiles ahead: ring must hold 3*NV+1 words plus
-  // 16-byte rounding at both ends.
-  static_assert(kR >= 3 * kNV + 16, "ring too small for two-tile lookahead");
-  static constexpr size_t kRingWords = (BSR ? 4 : 2) * size_t(kR);
-  static constexpr size_t kOutWords = MAT ? (BSR ? 2 : 1) * size_t(kNV) : 0;
-  static constexpr size_t kSmemBytes = (kRingWords + kOutWords) * 4;
+  static_assert(C % (4 * NT) == 0 || (4 * NT) % C == 0, "chunk / block shape");
+  static_assert(C % 4 == 0 && BMW % (4 * NT) == 0, "16-byte groups");
+  static_assert(NS >= 2, "need at least double buffering");
+  static constexpr int kSlotWords = NS * C;                    // per stream
+  static constexpr int kStreams = BSR ? 4 : 2;                 // keys (+ states)
+  static constexpr size_t kSmemBytes =
+      (size_t(kStreams) * kSlotWords + 2 * size_t(BMW)) * 4;
+  // values (arrays: one bit each) or bases (BSR: one state word each) per window
+  static constexpr uint32_t kWindow = BSR ? uint32_t(BMW) : uint32_t(BMW) * 32u;
+  static constexpr int kTile = C;  // elements per chunk, for grid sizing
 };
 
-// Producer-side state of one staged array.
-struct RingFeed {
-  const uint32_t *al;  // 16-byte aligned base (element index -off)
-  uint64_t n;          // element count
-  uint32_t off;        // misalignment of element 0, in words (0..3)
-  uint64_t front;      // aligned coordinate loaded so far (exclusive)
+// One input's run [s, e) streamed through NS slots of C words.  Chunk c
+// holds ring coordinates [c0 + c*C, c0 + (c+1)*C), where coordinate =
+// element index + off and off is the misalignment of element 0 within its
+// 16-byte group (so every chunk starts on a 16-byte boundary).
+struct Stream {
+  const uint32_t *al;    // 16-byte aligned base (coordinate 0)
+  const uint32_t *al_s;  // states (BSR), same misalignment
+  uint64_t n;            // array length
+  uint64_t s, e;         // element run of this CTA
+  uint64_t c0;           // coordinate of chunk 0
+  uint32_t off;
+  uint32_t nc;           // chunks covering the run
 };
 
-__device__ __forceinline__ RingFeed make_feed(const uint32_t *p, uint64_t n,
-                                              uint64_t first_elem) {
-  RingFeed f;
-  const uintptr_t addr = reinterpret_cast<uintptr_t>(p);
-  f.off = uint32_t((addr >> 2) & 3);
-  f.al = reinterpret_cast<const uint32_t *>(addr & ~uintptr_t(15));
-  f.n = n;
-  f.front = (first_elem + f.off) & ~uint64_t(3);
-  return f;
+template <int C>
+__device__ __forceinline__ Stream make_stream(const uint32_t *keys,
+                                              const uint32_t *states,
+                                              uint64_t n, uint64_t s,
+                                              uint64_t e) {
+  Stream x;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(keys);
+  x.off = uint32_t((a >> 2) & 3);
+  x.al = reinterpret_cast<const uint32_t *>(a & ~uintptr_t(15));
+  x.al_s = states ? reinterpret_cast<const uint32_t *>(
+                        reinterpret_cast<uintptr_t>(states) & ~uintptr_t(15))
+                  : nullptr;
+  x.n = n;
+  x.s = s;
+  x.e = e;
+  x.c0 = (s + x.off) & ~uint64_t(3);
+  x.nc = e > s ? uint32_t((e + x.off - x.c0 + C - 1) / C) : 0u;
+  return x;
 }
 
-// Bytes the bulk part of a feed step will move (for expect_tx), and the
-// aligned range.  Partial 16-byte chunks (only the chunk holding element 0
-// when the array is misaligned and the chunk holding the last element) are
-// loaded with plain loads by the producer thread instead.
-struct FeedPlan {
-  uint64_t lo, hi;      // aligned coords [lo, hi) to load this step
-  uint64_t blo, bhi;    // bulk sub-range (multiples of 4)
-};
-
-__device__ __forceinline__ FeedPlan plan_feed(const RingFeed &f,
-                                              uint64_t target_elem) {
-  FeedPlan pl;
-  const uint64_t end_al = f.n + f.off;
-  uint64_t t = (target_elem + f.off + 3) & ~uint64_t(3);
-  if (t > end_al) t = end_al;
-  pl.lo = f.front;
-  pl.hi = t > f.front ? t : f.front;
-  pl.blo = (pl.lo + 3) & ~uint64_t(3);
-  if (pl.blo < f.off) pl.blo = 4;  // chunk 0 is partial when off > 0
-  pl.bhi = pl.hi & ~uint64_t(3);
-  if (pl.bhi < pl.blo) pl.bhi = pl.blo;
-  return pl;
-}
-
-template <uint32_t R>
-__device__ __forceinline__ void run_feed(RingFeed &f, const FeedPlan &pl,
-                                         uint32_t *ring, uint64_t *bar,
-                                         uint64_t pol) {
-  constexpr uint32_t RM = R - 1;
-  if (pl.hi <= pl.lo) return;
-  // Plain loads for the (at most 3 + 3) aligned coords outside the bulk
-  // range: the head chunk when element 0 is misaligned, the tail chunk when
-  // the array end is.  Coordinates below `off` precede element 0.
-  const uint64_t hcut = pl.blo < pl.hi ? pl.blo : pl.hi;
-  for (uint64_t c = pl.lo; c < hcut; ++c)
-    if (c >= f.off) ring[c & RM] = __ldg(f.al + c);
-  const uint64_t tstart = pl.bhi > hcut ? pl.bhi : hcut;
-  for (uint64_t c = tstart; c < pl.hi; ++c)
-    if (c >= f.off) ring[c & RM] = __ldg(f.al + c);
-  if (pl.bhi > pl.blo) {
-    const uint32_t words = uint32_t(pl.bhi - pl.blo);
-    const uint32_t s0 = uint32_t(pl.blo) & RM;
-    const uint32_t first = (s0 + words <= R) ? words : (R - s0);
-    bulk_g2s(ring + s0, f.al + pl.blo, first * 4, bar, pol);
-    if (first < words)
-      bulk_g2s(ring, f.al + pl.blo + first, (words - first) * 4, bar, pol);
+// Loads chunk c of x into slot words `dst` (and `dst_s` for states),
+// completing on `bar`.  One thread.  Only the run's 16-byte groups are
+// copied; groups that are partly outside the array (first group when the
+// array is misaligned, last group at the array end) are loaded with plain
+// loads, so nothing outside the array is read.
+template <int C>
+__device__ __forceinline__ void issue_chunk(const Stream &x, uint32_t c,
+                                            uint32_t *dst, uint32_t *dst_s,
+                                            uint64_t *bar, uint64_t pol) {
+  const uint64_t lo = x.c0 + uint64_t(c) * C;
+  uint64_t hi = lo + C;
+  const uint64_t need = (x.e + x.off + 3) & ~uint64_t(3);
+  if (hi > need) hi = need;
+  const uint64_t arr_end = x.n + x.off;
+  uint64_t blo = lo;
+  if (blo < 4 && x.off > 0) blo = 4;  // group 0 is partial
+  uint64_t bhi = arr_end & ~uint64_t(3);
+  if (bhi > hi) bhi = hi;
+  if (bhi < blo) bhi = blo;
+  // head [lo, blo) and tail [bhi, hi): at most 3 + 3 words
+  const uint64_t hcut = blo < hi ? blo : hi;
+  for (uint64_t q = lo; q < hcut; ++q)
+    if (q >= x.off && q < arr_end) {
+      dst[q - lo] = __ldg(x.al + q);
+      if (dst_s) dst_s[q - lo] = __ldg(x.al_s + q);
+    }
+  for (uint64_t q = (bhi > hcut ? bhi : hcut); q < hi; ++q)
+    if (q >= x.off && q < arr_end) {
+      dst[q - lo] = __ldg(x.al + q);
+      if (dst_s) dst_s[q - lo] = __ldg(x.al_s + q);
+    }
+  const uint32_t bytes = uint32_t(bhi - blo) * 4u;
+  // order the block's earlier generic-proxy reads of this slot (made visible
+  // to this thread by the barrier before the refill) before the async-proxy
+  // writes of the bulk copy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_arrive_expect_tx(bar, dst_s ? 2 * bytes : bytes);
+  if (bytes) {
+    bulk_g2s(dst + (blo - lo), x.al + blo, bytes, bar, pol);
+    if (dst_s) bulk_g2s(dst_s + (blo - lo), x.al_s + blo, bytes, bar, pol);
   }
-  f.front = pl.hi;
 }
 
-__device__ __forceinline__ uint32_t plan_bytes(const FeedPlan &pl) {
-  return uint32_t(pl.bhi - pl.blo) * 4;
+// Merge-path co-ranks of two diagonals at once: threads [0, NT/2) search
+// d0, threads [NT/2, NT) search d1, each probing 2 points per round
+// ((NT+1)-ary narrowing; 3 rounds for 2^24-element inputs).  The co-rank of
+// diagonal d is the smallest i with A[i] > B[d-1-i] (A first on ties).
+template <int NT>
+__device__ __forceinline__ void corank_pair(const uint32_t *A, uint64_t na,
+                                            const uint32_t *B, uint64_t nb,
+                                            uint64_t d0, uint64_t d1,
+                                            uint64_t *i0, uint64_t *i1) {
+  constexpr int H = NT / 2;
+  constexpr uint64_t F = 2 * H + 1;  // fan-out per round
+  __shared__ uint32_t cnt[2];
+  const int t = threadIdx.x;
+  const int half = t >= H;
+  const uint32_t ti = uint32_t(t - half * H);
+  const uint64_t d = half ? d1 : d0;
+  uint64_t lo = d > nb ? d - nb : 0;
+  uint64_t hi = d < na ? d : na;
+  for (;;) {
+    if (t == 0) {
+      cnt[0] = 0;
+      cnt[1] = 0;
+    }
+    __syncthreads();
+    const uint64_t span = hi - lo;
+    uint32_t pr = 0;
+    if (span > 0) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint64_t k = uint64_t(2 * ti + j);
+        uint64_t x;
+        bool ok;
+        if (span < F) {
+          x = lo + k;
+          ok = k < span;
+        } else {
+          x = lo + ((k + 1) * span) / F;
+          ok = true;
+        }
+        if (ok && __ldg(A + x) <= __ldg(B + (d - 1 - x))) ++pr;
+      }
+    }
+    const unsigned bal1 = __ballot_sync(0xffffffffu, pr >= 1);
+    const unsigned bal2 = __ballot_sync(0xffffffffu, pr >= 2);
+    if ((t & 31) == 0 && (bal1 | bal2))
+      atomicAdd(&cnt[half], __popc(bal1) + __popc(bal2));
+    __syncthreads();
+    const uint64_t c = cnt[half];
+    if (span > 0) {
+      if (span < F) {
+        lo += c;
+        hi = lo;
+      } else {
+        const uint64_t nhi = (c < F - 1) ? lo + ((c + 1) * span) / F : hi;
+        if (c > 0) lo = lo + (c * span) / F + 1;
+        hi = nhi;
+      }
+    }
+    if (__syncthreads_and(hi == lo)) break;
+  }
+  *i0 = half ? 0 : lo;
+  *i1 = half ? lo : 0;
+  // broadcast each half's answer to the whole block
+  __shared__ unsigned long long res[2];
+  if (t == 0) res[0] = lo;
+  if (t == H) res[1] = lo;
+  __syncthreads();
+  *i0 = res[0];
+  *i1 = res[1];
 }
 
-template <int NT, int VT, int RLOG, bool BSR, bool MAT>
-__global__ void __launch_bounds__(NT)
+// Occupancy target for register allocation: the shared-memory footprint
+// allows at most this many CTAs per SM anyway.
+template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
+constexpr int merge_min_blocks() {
+  constexpr size_t smem = MergeCfg<NT, C, NS, BMW, BSR, MAT>::kSmemBytes + 1024;
+  constexpr int by_smem = int((228 * 1024) / smem);
+  constexpr int by_threads = 2048 / NT;
+  constexpr int b = by_smem < by_threads ? by_smem : by_threads;
+  return b < 1 ? 1 : b;
+}
+
+template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
+__global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT>()))
     merge_kernel(const MergeArgs p) {
-  using Cfg = MergeCfg<NT, VT, RLOG, BSR, MAT>;
-  constexpr int NV = Cfg::kNV;
-  constexpr uint32_t R = Cfg::kR;
-  constexpr uint32_t RM = R - 1;
+  using Cfg = MergeCfg<NT, C, NS, BMW, BSR, MAT>;
+  constexpr uint32_t WIN = Cfg::kWindow;
+  constexpr int GPC = C / 4;          // 16-byte groups per chunk
+  constexpr int WPT = BMW / NT;       // table words per thread (AND phase)
 
   extern __shared__ __align__(128) uint32_t smem[];
-  uint32_t *ringA = smem;
-  uint32_t *ringB = smem + R;
-  uint32_t *ringSA = BSR ? smem + 2 * R : nullptr;
-  uint32_t *ringSB = BSR ? smem + 3 * R : nullptr;
-  uint32_t *sOut = smem + Cfg::kRingWords;
-  uint32_t *sOutS = sOut + NV;
+  uint32_t *slotA = smem;
+  uint32_t *slotB = smem + Cfg::kSlotWords;
+  uint32_t *slotSA = BSR ? smem + 2 * Cfg::kSlotWords : nullptr;
+  uint32_t *slotSB = BSR ? smem + 3 * Cfg::kSlotWords : nullptr;
+  uint32_t *tabA = smem + Cfg::kStreams * Cfg::kSlotWords;
+  uint32_t *tabB = tabA + BMW;
 
-  __shared__ __align__(8) uint64_t mbar[2];
-  __shared__ uint32_t sCo[NT + 1];
+  __shared__ __align__(8) uint64_t barA[NS];
+  __shared__ __align__(8) uint64_t barB[NS];
   __shared__ uint32_t warp_sums[NT / 32];
   __shared__ uint32_t s_vid;
-  __shared__ int s_abort;
+  __shared__ uint32_t s_bound[3];  // by pass, triple-buffered
+  __shared__ unsigned long long red[NT / 32];
+  __shared__ unsigned long long s_excl;
+  __shared__ uint32_t s_edge[4];
 
   const int t = threadIdx.x;
+  const int lane = t & 31;
 
   // ---- problem (A = smaller set) ----
   uint64_t na = p.na_dev ? *p.na_dev : p.na;
@@ -186,239 +284,356 @@ __global__ void __launch_bounds__(NT)
 
   if (t == 0) {
     s_vid = atomicAdd(&p.sync->ticket, 1u);
-    s_abort = 0;
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+    for (int i = 0; i < NS; ++i) {
+      mbar_init(&barA[i], 1);
+      mbar_init(&barB[i], 1);
+    }
     fence_mbar_init();
   }
+  for (int i = t; i < 2 * BMW; i += NT) tabA[i] = 0;  // tabA and tabB
   __syncthreads();
   const uint32_t vid = s_vid;
   const uint32_t G = gridDim.x;
   uint64_t D = (total + G - 1) / G;
-  D = ((D + NV - 1) / NV) * NV;  // whole tiles per CTA where possible
+  D = ((D + C - 1) / C) * C;
   const uint64_t d0 = (uint64_t(vid) * D < total) ? uint64_t(vid) * D : total;
   const uint64_t d1 = (d0 + D < total) ? d0 + D : total;
 
-  // ---- 1. co-rank of diagonal d0: smallest i with A[i] > B[d0-1-i] ----
-  uint64_t lo = d0 > nb ? d0 - nb : 0;
-  uint64_t hi = d0 < na ? d0 : na;
-  while (hi > lo) {
-    const uint64_t span = hi - lo;
-    if (span <= uint64_t(NT)) {
-      bool pr = false;
-      if (uint64_t(t) < span) {
-        const uint64_t x = lo + t;
-        pr = __ldg(A + x) <= __ldg(B + (d0 - 1 - x));
-      }
-      lo += uint64_t(__syncthreads_count(pr));
-      break;
-    }
-    const uint64_t x = lo + (uint64_t(t + 1) * span) / (NT + 1);
-    const bool pr = __ldg(A + x) <= __ldg(B + (d0 - 1 - x));
-    const uint64_t c = uint64_t(__syncthreads_count(pr));
-    const uint64_t nhi = (c < NT) ? lo + ((c + 1) * span) / (NT + 1) : hi;
-    if (c > 0) lo = lo + (c * span) / (NT + 1) + 1;
-    hi = nhi;
-  }
-  uint64_t ia = lo, ib = d0 - lo;
-  const uint64_t stage_base = ia;  // exclusive stage region of this CTA
+  // ---- 1. this CTA's runs: A[ia0, ia1) and B[ib0, ib1] ----
+  uint64_t ia0, ia1;
+  corank_pair<NT>(A, na, B, nb, d0, d1, &ia0, &ia1);
+  const uint64_t ib0 = d0 - ia0;
+  const uint64_t ib1 = d1 - ia1;
+  // B[ib1] is the one element past the range that can match A[ia1-1]
+  const uint64_t be = ib1 < nb ? ib1 + 1 : nb;
+  const uint64_t stage_base = ia0;  // matches <= owned A elements
+  const bool work = ia1 > ia0 && be > ib0;
 
-  // ---- 2. stream tiles ----
   const uint64_t pol = l2_evict_first_policy();
-  RingFeed fA = make_feed(A, na, ia), fB = make_feed(B, nb, ib);
-  RingFeed fSA, fSB;
-  if (BSR) {
-    fSA = make_feed(SA, na, ia);
-    fSB = make_feed(SB, nb, ib);
-  }
-  // state-ring slot = key-ring slot + (state misalignment - key misalignment)
-  const uint32_t dSA = BSR ? (fSA.off - fA.off) : 0;
-  const uint32_t dSB = BSR ? (fSB.off - fB.off) : 0;
-
-  // Producer: stage everything this CTA needs up to element targets.
-  auto issue = [&](int bar_idx, uint64_t ia_n, uint64_t ib_n, uint64_t dn) {
-    const uint64_t rem = d1 - dn;  // merged elements left after ia_n/ib_n
-    uint64_t ta = ia_n + (rem < 2 * uint64_t(NV) ? rem : 2 * uint64_t(NV)) + 1;
-    uint64_t tb = ib_n + (rem < 2 * uint64_t(NV) ? rem : 2 * uint64_t(NV)) + 1;
-    if (ta > na) ta = na;
-    if (tb > nb) tb = nb;
-    FeedPlan pa = plan_feed(fA, ta), pb = plan_feed(fB, tb);
-    FeedPlan psa, psb;
-    uint32_t bytes = plan_bytes(pa) + plan_bytes(pb);
-    if (BSR) {
-      psa = plan_feed(fSA, ta);
-      psb = plan_feed(fSB, tb);
-      bytes += plan_bytes(psa) + plan_bytes(psb);
+  Stream xa = make_stream<C>(A, BSR ? SA : nullptr, na, ia0, work ? ia1 : ia0);
+  Stream xb = make_stream<C>(B, BSR ? SB : nullptr, nb, ib0, work ? be : ib0);
+  uint32_t issuedA = 0, issuedB = 0;  // chunks issued (thread 0's view)
+  if (t == 0) {
+    for (; issuedA < xa.nc && issuedA < uint32_t(NS); ++issuedA)
+      issue_chunk<C>(xa, issuedA, slotA + (issuedA % NS) * C,
+                     BSR ? slotSA + (issuedA % NS) * C : nullptr,
+                     &barA[issuedA % NS], pol);
+    for (; issuedB < xb.nc && issuedB < uint32_t(NS); ++issuedB)
+      issue_chunk<C>(xb, issuedB, slotB + (issuedB % NS) * C,
+                     BSR ? slotSB + (issuedB % NS) * C : nullptr,
+                     &barB[issuedB % NS], pol);
+    // first / last values of both runs decide dense vs sparse handling
+    if (work) {
+      s_edge[0] = __ldg(A + ia0);
+      s_edge[1] = __ldg(A + ia1 - 1);
+      s_edge[2] = __ldg(B + ib0);
+      s_edge[3] = __ldg(B + be - 1);
     }
-    mbar_arrive_expect_tx(&mbar[bar_idx], bytes);
-    run_feed<R>(fA, pa, ringA, &mbar[bar_idx], pol);
-    run_feed<R>(fB, pb, ringB, &mbar[bar_idx], pol);
-    if (BSR) {
-      run_feed<R>(fSA, psa, ringSA, &mbar[bar_idx], pol);
-      run_feed<R>(fSB, psb, ringSB, &mbar[bar_idx], pol);
+  }
+  __syncthreads();
+
+  uint32_t ca = 0, cb = 0;  // current chunk of each stream
+  bool aborted = false;
+  uint64_t cnt = 0;      // count mode (BSR: elements)
+  uint64_t cta_cnt = 0;  // materialise: matches staged so far
+
+  // Valid slot-index range of chunk c of stream x.
+  auto qrange = [&](const Stream &x, uint32_t c, uint32_t &q0, uint32_t &q1) {
+    const uint64_t cs = x.c0 + uint64_t(c) * C;
+    const uint64_t vs = x.s + x.off, ve = x.e + x.off;
+    q0 = vs > cs ? uint32_t(vs - cs) : 0u;
+    q1 = ve < cs + C ? uint32_t(ve - cs) : uint32_t(C);
+  };
+  // Waits (all threads) for chunk c of a stream; false on timeout.
+  auto wait_chunk = [&](uint64_t *bars, uint32_t c) -> bool {
+    const bool ok = mbar_wait_bounded(&bars[c % NS], (c / NS) & 1u, p.err);
+    return !__syncthreads_or(!ok);
+  };
+  // Releases chunk c's slot (call after a barrier) and loads chunk c + NS.
+  auto refill = [&](const Stream &x, uint32_t *slots, uint32_t *slots_s,
+                    uint64_t *bars, uint32_t c, uint32_t &issued) {
+    if (t == 0 && c + NS < x.nc) {
+      const uint32_t nx = c + NS;
+      issue_chunk<C>(x, nx, slots + (nx % NS) * C,
+                     BSR ? slots_s + (nx % NS) * C : nullptr, &bars[nx % NS],
+                     pol);
+      issued = nx + 1;
     }
   };
 
-  uint64_t diag = ia + ib;
-  const bool has_work = diag < d1;
-  if (has_work && t == 0) issue(0, ia, ib, diag);  // batch -1 -> barrier 0
-  __syncthreads();
-
-  uint64_t cnt = 0;      // count mode: this thread's matches
-  uint64_t cta_cnt = 0;  // materialise: matches staged by this CTA
-  int k = 0;             // tile index
-  bool aborted = false;
-  while (diag < d1) {
-    // wait for the batch that completes this tile's window
-    {
-      int wb = -2;  // which batch: -1 for tile 0, k-2 for k >= 2
-      if (k == 0) wb = -1;
-      else if (k >= 2) wb = k - 2;
-      if (wb >= -1) {
-        const int bi = (wb + 1) & 1;
-        const uint32_t par = uint32_t((wb + 1) >> 1) & 1u;
-        const bool ok = mbar_wait_bounded(&mbar[bi], par, p.err);
-        if (__syncthreads_or(!ok)) {
-          aborted = true;
-          break;
-        }
-      }
-    }
-    const uint64_t rem = d1 - diag;
-    const uint32_t nvt = rem < uint64_t(NV) ? uint32_t(rem) : uint32_t(NV);
-    const uint32_t la = (na - ia) < nvt ? uint32_t(na - ia) : nvt;
-    const uint32_t lb = (nb - ib) < nvt ? uint32_t(nb - ib) : nvt;
-    const uint32_t abase = uint32_t(ia + fA.off);
-    const uint32_t bbase = uint32_t(ib + fB.off);
-
-    // ---- split: co-rank of each thread's sub-diagonal within the window ----
-    {
-      // thread 0's own diagonal is 0; it computes the tile end instead
-      const uint32_t d = (t == 0) ? nvt : min(uint32_t(t) * VT, nvt);
-      uint32_t l = d > lb ? d - lb : 0, h = d < la ? d : la;
-      while (l < h) {
-        const uint32_t m = (l + h) >> 1;
-        const uint32_t av = ringA[(abase + m) & RM];
-        const uint32_t bv = ringB[(bbase + d - 1 - m) & RM];
-        if (av <= bv) l = m + 1; else h = m;
-      }
+  if (work) {
+    const uint32_t a_first = s_edge[0], a_last = s_edge[1];
+    const uint32_t b_first = s_edge[2], b_last = s_edge[3];
+    const uint32_t vmin = a_first < b_first ? a_first : b_first;
+    const uint32_t vmax = a_last > b_last ? a_last : b_last;
+    const uint64_t elems = (ia1 - ia0) + (be - ib0);
+    // dense when a window table pays for itself: at least one element per
+    // 64 values (arrays) / per 2 bases (BSR) over the run's value span
+    const bool dense = BSR ? (2 * elems >= uint64_t(vmax - vmin) + 1)
+                           : (64 * elems >= uint64_t(vmax - vmin) + 1);
+    if (dense) {
+      // ================= dense: value windows =================
+      // Per stream: current chunk and cursor (slot index of its first
+      // unconsumed element).  Window [w, w + wlen) takes a prefix of what is
+      // left of each stream; w is the smaller of the two cursor values.
+      if (!wait_chunk(barA, 0) || !wait_chunk(barB, 0)) aborted = true;
+      uint32_t qa0, qa1, qb0, qb1;
+      qrange(xa, 0, qa0, qa1);
+      qrange(xb, 0, qb0, qb1);
+      uint32_t curA = qa0, curB = qb0;
+      bool doneA = false, doneB = false;
+      uint32_t pass = 0;
       if (t == 0) {
-        sCo[NT] = l;
-        sCo[0] = 0;
-      } else {
-        sCo[t] = l;
+        s_bound[0] = 0xffffffffu;
+        s_bound[1] = 0xffffffffu;
+        s_bound[2] = 0xffffffffu;
       }
-    }
-    __syncthreads();
-    const uint32_t ca = sCo[NT], cb = nvt - ca;
-    // ---- producer: next batch (barrier (k+1)&1) ----
-    if (t == 0) issue((k + 1) & 1, ia + ca, ib + cb, diag + nvt);
-
-    // ---- serial merge of this thread's VT steps ----
-    const uint32_t dt = min(uint32_t(t) * VT, nvt);
-    const uint32_t dn = min(uint32_t(t + 1) * VT, nvt);
-    const uint32_t i0 = sCo[t];
-    const uint32_t j0 = dt - i0;
-    uint32_t as = (abase + i0) & RM, bs = (bbase + j0) & RM;
-    uint32_t av = ringA[as], bv = ringB[bs];
-    uint32_t c = 0;
-    const bool fast = (nvt == uint32_t(NV)) && (ia + NV + 1 <= na) &&
-                      (ib + NV + 1 <= nb);
-    auto on_match = [&](uint32_t key) {
-      if (BSR) {
-        const uint32_t st = ringSA[(as + dSA) & RM] & ringSB[(bs + dSB) & RM];
-        if (st != 0) {
-          if (MAT) {
-            sOut[t * VT + c] = key;
-            sOutS[t * VT + c] = st;
+      __syncthreads();
+      while (!aborted) {
+        const uint32_t va = slotA[(ca % NS) * C + curA];
+        const uint32_t vb = slotB[(cb % NS) * C + curB];
+        const uint32_t w = va < vb ? va : vb;
+        const uint32_t wlen =
+            (uint64_t(w) + WIN > 0x100000000ull) ? uint32_t(0x100000000ull - w) : WIN;
+#pragma unroll 1
+        for (int sidx = 0; sidx < 2 && !aborted; ++sidx) {
+          const bool isA = sidx == 0;
+          const Stream &x = isA ? xa : xb;
+          uint32_t *slots = isA ? slotA : slotB;
+          uint32_t *slots_s = isA ? slotSA : slotSB;
+          uint64_t *bars = isA ? barA : barB;
+          uint32_t *tab = isA ? tabA : tabB;
+          uint32_t &c = isA ? ca : cb;
+          uint32_t &cur = isA ? curA : curB;
+          bool &done = isA ? doneA : doneB;
+          uint32_t &issued = isA ? issuedA : issuedB;
+          for (;;) {
+            const uint32_t *sl = slots + (c % NS) * C;
+            const uint32_t *sls = BSR ? slots_s + (c % NS) * C : nullptr;
+            uint32_t q0, q1;
+            qrange(x, c, q0, q1);
+            // every element from the cursor on is >= w; insert the prefix
+            // below w + wlen, each thread stopping at its first element past it
+            uint32_t stop = 0xffffffffu;
+            const uint32_t g1 = (q1 + 3) >> 2;
+            for (uint32_t g = (cur >> 2) + t; g < g1; g += NT) {
+              const uint4 v4 = reinterpret_cast<const uint4 *>(sl)[g];
+              const uint32_t vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+              for (int e2 = 0; e2 < 4; ++e2) {
+                const uint32_t q = 4 * g + e2;
+                if (q < cur || q >= q1) continue;
+                const uint32_t o = vv[e2] - w;
+                if (o < wlen) {
+                  if (BSR) tab[o] = sls[q];
+                  else atomicOr(&tab[o >> 5], 1u << (o & 31u));
+                } else if (stop == 0xffffffffu) {
+                  stop = q;
+                }
+              }
+              if (stop != 0xffffffffu) break;
+            }
+            const uint32_t wstop = __reduce_min_sync(0xffffffffu, stop);
+            if (lane == 0 && wstop != 0xffffffffu) atomicMin(&s_bound[pass % 3], wstop);
+            __syncthreads();  // chunk reads and s_bound done
+            const uint32_t bnd = s_bound[pass % 3];
+            if (t == 0) s_bound[(pass + 2) % 3] = 0xffffffffu;
+            ++pass;
+            if (bnd != 0xffffffffu) {  // the window ends inside this chunk
+              cur = bnd;
+              break;
+            }
+            refill(x, slots, slots_s, bars, c, issued);
             ++c;
-          } else {
-            cnt += __popc(st);
+            if (c >= x.nc) {
+              done = true;
+              break;
+            }
+            if (!wait_chunk(bars, c)) {
+              aborted = true;
+              break;
+            }
+            uint32_t n0, n1;
+            qrange(x, c, n0, n1);
+            cur = n0;
           }
         }
-      } else {
-        if (MAT) sOut[t * VT + c] = key;
-        ++c;
-      }
-    };
-    if (fast) {
+        if (aborted) break;
+        // AND the two tables and clear them; thread t owns words
+        // [t*WPT, (t+1)*WPT), so matches come out in ascending order
+        uint32_t hits = 0;
+        uint32_t myw[WPT];
 #pragma unroll
-      for (int s = 0; s < VT; ++s) {
-        const bool takeA = av <= bv;
-        if (av == bv) on_match(av);
-        if (takeA) {
-          as = (as + 1) & RM;
-          av = ringA[as];
-        } else {
-          bs = (bs + 1) & RM;
-          bv = ringB[bs];
+        for (int j = 0; j < WPT; j += 4) {
+          uint4 *pa = reinterpret_cast<uint4 *>(tabA + t * WPT) + j / 4;
+          uint4 *pb = reinterpret_cast<uint4 *>(tabB + t * WPT) + j / 4;
+          const uint4 x4 = *pa, y4 = *pb;
+          *pa = make_uint4(0, 0, 0, 0);
+          *pb = make_uint4(0, 0, 0, 0);
+          myw[j] = x4.x & y4.x;
+          myw[j + 1] = x4.y & y4.y;
+          myw[j + 2] = x4.z & y4.z;
+          myw[j + 3] = x4.w & y4.w;
         }
-      }
-    } else {
-      uint64_t gi = ia + i0, gj = ib + j0;
-      const uint32_t steps = dn - dt;
 #pragma unroll
-      for (int s = 0; s < VT; ++s) {
-        if (uint32_t(s) < steps) {
-          const bool aok = gi < na, bok = gj < nb;
-          const bool takeA = aok && (!bok || av <= bv);
-          if (takeA && bok && av == bv) on_match(av);
-          if (takeA) {
-            ++gi;
-            as = (as + 1) & RM;
-            av = ringA[as];
+        for (int j = 0; j < WPT; ++j) {
+          if (BSR) {
+            if (MAT) hits += (myw[j] != 0);
+            else cnt += __popc(myw[j]);
           } else {
-            ++gj;
-            bs = (bs + 1) & RM;
-            bv = ringB[bs];
+            hits += __popc(myw[j]);
           }
         }
+        if (MAT) {
+          // block scan only for windows that have matches
+          if (__syncthreads_or(hits != 0)) {
+            uint32_t tot;
+            const uint32_t ex = block_exclusive_scan<NT>(hits, warp_sums, &tot);
+            if (hits) {
+              uint32_t *dst = p.stage + stage_base + cta_cnt + ex;
+              uint32_t *dsts = BSR ? p.stage_s + stage_base + cta_cnt + ex : nullptr;
+              uint32_t o = 0;
+#pragma unroll
+              for (int j = 0; j < WPT; ++j) {
+                uint32_t m = myw[j];
+                const uint32_t wbase = w + uint32_t(t * WPT + j) * (BSR ? 1u : 32u);
+                if (BSR) {
+                  if (m) {
+                    dst[o] = wbase;
+                    dsts[o] = m;
+                    ++o;
+                  }
+                } else {
+                  while (m) {
+                    dst[o++] = wbase + uint32_t(__ffs(m) - 1);
+                    m &= m - 1;
+                  }
+                }
+              }
+            }
+            cta_cnt += tot;
+          }
+        } else if (!BSR) {
+          cnt += hits;
+        }
+        __syncthreads();  // tables clear before the next window's inserts
+        // one run used up: nothing left in the other can match
+        if (doneA || doneB) break;
+        if (uint64_t(w) + wlen >= 0x100000000ull) break;
       }
-    }
-
-    if (MAT) {
-      uint32_t tot;
-      const uint32_t ex = block_exclusive_scan<NT>(c, warp_sums, &tot);
-      uint32_t *dst = p.stage + stage_base + cta_cnt + ex;
-      for (uint32_t q = 0; q < c; ++q) dst[q] = sOut[t * VT + q];
-      if (BSR) {
-        uint32_t *dsts = p.stage_s + stage_base + cta_cnt + ex;
-        for (uint32_t q = 0; q < c; ++q) dsts[q] = sOutS[t * VT + q];
-      }
-      cta_cnt += tot;
     } else {
-      if (!BSR) cnt += c;
-      __syncthreads();  // sCo is rewritten by the next split
+      // ============ sparse: chunk pairs, binary search of A in B ============
+      if (!wait_chunk(barA, 0) || !wait_chunk(barB, 0)) aborted = true;
+      while (!aborted) {
+        const uint32_t *sa = slotA + (ca % NS) * C;
+        const uint32_t *ssa = BSR ? slotSA + (ca % NS) * C : nullptr;
+        const uint32_t *sb = slotB + (cb % NS) * C;
+        const uint32_t *ssb = BSR ? slotSB + (cb % NS) * C : nullptr;
+        uint32_t qa0, qa1, qb0, qb1;
+        qrange(xa, ca, qa0, qa1);
+        qrange(xb, cb, qb0, qb1);
+        const uint32_t bmin = sb[qb0], bmax = sb[qb1 - 1];
+        const uint32_t amax = sa[qa1 - 1];
+        // thread t: contiguous A elements [qa0 + t*per, ...) in order
+        constexpr uint32_t PER = (C + NT - 1) / NT;
+        const uint32_t my0 = qa0 + uint32_t(t) * PER;
+        uint32_t hits = 0;
+        auto find = [&](uint32_t v, uint32_t &st) -> bool {
+          if (v < bmin || v > bmax) return false;
+          uint32_t lo = qb0, len = qb1 - qb0;
+          while (len > 0) {
+            const uint32_t h = len >> 1;
+            if (sb[lo + h] < v) {
+              lo += h + 1;
+              len -= h + 1;
+            } else {
+              len = h;
+            }
+          }
+          if (lo >= qb1 || sb[lo] != v) return false;
+          if (BSR) st = ssb[lo];
+          return true;
+        };
+        for (uint32_t i = 0; i < PER; ++i) {
+          const uint32_t q = my0 + i;
+          if (q >= qa1) break;
+          uint32_t st = 0;
+          if (find(sa[q], st)) {
+            if (BSR) {
+              st &= ssa[q];
+              if (st) {
+                if (MAT) ++hits;
+                else cnt += __popc(st);
+              }
+            } else {
+              ++hits;
+            }
+          }
+        }
+        if (MAT) {
+          uint32_t tot;
+          const uint32_t ex = block_exclusive_scan<NT>(hits, warp_sums, &tot);
+          if (hits) {
+            uint32_t *dst = p.stage + stage_base + cta_cnt + ex;
+            uint32_t *dsts = BSR ? p.stage_s + stage_base + cta_cnt + ex : nullptr;
+            uint32_t o = 0;
+            for (uint32_t i = 0; i < PER; ++i) {
+              const uint32_t q = my0 + i;
+              if (q >= qa1) break;
+              uint32_t st = 0;
+              if (find(sa[q], st)) {
+                if (BSR) {
+                  st &= ssa[q];
+                  if (st) {
+                    dst[o] = sa[q];
+                    dsts[o] = st;
+                    ++o;
+                  }
+                } else {
+                  dst[o++] = sa[q];
+                }
+              }
+            }
+          }
+          cta_cnt += tot;
+        } else if (!BSR) {
+          cnt += hits;
+        }
+        __syncthreads();  // chunk reads done
+        const bool advA = amax <= bmax, advB = bmax <= amax;
+        if (advA) {
+          refill(xa, slotA, slotSA, barA, ca, issuedA);
+          ++ca;
+        }
+        if (advB) {
+          refill(xb, slotB, slotSB, barB, cb, issuedB);
+          ++cb;
+        }
+        if (ca >= xa.nc || cb >= xb.nc) break;
+        if (advA && !wait_chunk(barA, ca)) { aborted = true; break; }
+        if (advB && !wait_chunk(barB, cb)) { aborted = true; break; }
+      }
     }
-    ia += ca;
-    ib += cb;
-    diag += nvt;
-    ++k;
   }
 
-  // ---- drain: no bulk copy may still target this CTA's shared memory ----
-  if (has_work && t == 0) {
-    // Batches issued: -1 .. k-1.  Tile 0 waited for -1, tile j >= 2 for j-2,
-    // so k-2 .. k-1 (or -1 alone, if tile 0's wait timed out) may still be
-    // in flight.  Each barrier has at most one phase outstanding.
-    const int first = (k == 0) ? -1 : (k >= 2 ? k - 2 : 0);
-    const int last = (k == 0) ? -1 : k - 1;
-    for (int wb = first; wb <= last; ++wb) {
-      mbar_wait_bounded(&mbar[(wb + 1) & 1], uint32_t((wb + 1) >> 1) & 1u,
-                        p.err);
-    }
+  // ---- drain: every issued chunk must have landed before exit ----
+  if (t == 0) {
+    // chunks [first unwaited, issued) may still be in flight
+    const uint32_t fa = ca, fb = cb;
+    for (uint32_t c = fa; c < issuedA; ++c)
+      mbar_wait_bounded(&barA[c % NS], (c / NS) & 1u, p.err);
+    for (uint32_t c = fb; c < issuedB; ++c)
+      mbar_wait_bounded(&barB[c % NS], (c / NS) & 1u, p.err);
   }
   __syncthreads();
   if (aborted) return;
 
   // ---- 3. combine ----
   if (!MAT) {
-    // block reduction of cnt
     uint64_t v = cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __shared__ unsigned long long red[NT / 32];
-    if ((t & 31) == 0) red[t >> 5] = v;
+    if (lane == 0) red[t >> 5] = v;
     __syncthreads();
     if (t == 0) {
       unsigned long long s = 0;
@@ -437,13 +652,15 @@ __global__ void __launch_bounds__(NT)
     return;
   }
 
-  // materialise: decoupled look-back over CTA ranges
-  __shared__ unsigned long long s_excl;
-  if (t == 0) {
-    const uint64_t ex = lookback_exclusive(p.status, vid, cta_cnt, p.epoch, p.err);
-    s_excl = ex;
-    if (ex != UINT64_MAX && ex + cta_cnt > p.out_cap)
-      record_error(p.err, DEV_ERR_CAPACITY);
+  // materialise: decoupled look-back over CTA ranges (warp 0)
+  if (t < 32) {
+    const uint64_t ex =
+        lookback_exclusive_warp(p.status, vid, cta_cnt, p.epoch, p.err);
+    if (t == 0) {
+      s_excl = ex;
+      if (ex != UINT64_MAX && ex + cta_cnt > p.out_cap)
+        record_error(p.err, DEV_ERR_CAPACITY);
+    }
   }
   __syncthreads();
   const uint64_t ex = s_excl;
@@ -463,5 +680,4 @@ __global__ void __launch_bounds__(NT)
     }
   }
 }
-
 }  // namespace setops

@@ -89,7 +89,9 @@ int ctx_occupancy(setops_ctx *ctx, const KernelInfo &k, int *blocks) {
     *blocks = it->second;
     return SETOPS_OK;
   }
-  if (k.dyn_smem > 48 * 1024)
+  // opt in whenever dynamic shared memory is used: static plus dynamic
+  // shared memory above 48 KB needs it
+  if (k.dyn_smem > 0)
     CK(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             int(k.dyn_smem)));
   int n = 0;
@@ -208,14 +210,13 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // ratio < 32: merge-path; 32..511: thread-per-element search with four
-    // interleaved lookups; >= 512: one warp per element.
-    unsigned u = (b < 5)   ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
-                 : (b < 9) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
-                           : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3));
-    unsigned s = (b < 5)   ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
-                 : (b < 9) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
-                           : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
+    // ratio < 32: merge-path; 32..511: sampled thread-per-element search;
+    // 512..8191: 16 lanes per element; >= 8192: a warp per element.
+    unsigned v = (b < 5)    ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
+                 : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
+                 : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(1))
+                            : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
+    unsigned u = v, s = v;
     ctx->policy[0][b] = u;
     ctx->policy[1][b] = s;
   }
@@ -241,7 +242,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   } else {
     const uint64_t ntiles = (mn + k.tile - 1) / k.tile;
     grid = std::max<uint64_t>(1, std::min(full, ntiles));
-    status_words = std::max<uint64_t>(ntiles, 1);
+    status_words = grid;
   }
   if (j.grid_cap && grid > j.grid_cap) grid = j.grid_cap;
   uint32_t epoch = 0;
@@ -249,6 +250,15 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   RK(ctx_next_epoch(ctx, &epoch));
   LaunchSync *sync = ctx->sync + j.sync_slot;
 
+  uint32_t *stage = nullptr, *stage_s = nullptr;
+  if (mat) {
+    RK(buf_reserve(ctx, ctx->stage0, std::max<uint64_t>(mn, 1) * 4));
+    stage = static_cast<uint32_t *>(ctx->stage0.p);
+    if (j.bsr) {
+      RK(buf_reserve(ctx, ctx->stage1, std::max<uint64_t>(mn, 1) * 4));
+      stage_s = static_cast<uint32_t *>(ctx->stage1.p);
+    }
+  }
   if (j.choice.algo == ALGO_MERGE) {
     MergeArgs a{};
     a.a = j.a;
@@ -259,14 +269,8 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.nb = j.nb;
     a.na_dev = j.na_dev;
     a.nb_dev = j.nb_dev;
-    if (mat) {
-      RK(buf_reserve(ctx, ctx->stage0, std::max<uint64_t>(mn, 1) * 4));
-      a.stage = static_cast<uint32_t *>(ctx->stage0.p);
-      if (j.bsr) {
-        RK(buf_reserve(ctx, ctx->stage1, std::max<uint64_t>(mn, 1) * 4));
-        a.stage_s = static_cast<uint32_t *>(ctx->stage1.p);
-      }
-    }
+    a.stage = stage;
+    a.stage_s = stage_s;
     a.out = j.out;
     a.out_s = j.out_s;
     a.out_cap = j.out_cap;
@@ -278,8 +282,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.skip_rule = j.skip_rule;
     a.ratio_thr = j.ratio_thr;
     void *args[] = {&a};
-    CK(cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args,
-                        k.dyn_smem, ctx->st));
+    RK(ctx_launch(ctx, k, grid, args));
   } else {
     GallopArgs a{};
     a.a = j.a;
@@ -290,6 +293,8 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.nb = j.nb;
     a.na_dev = j.na_dev;
     a.nb_dev = j.nb_dev;
+    a.stage = stage;
+    a.stage_s = stage_s;
     a.out = j.out;
     a.out_s = j.out_s;
     a.out_cap = j.out_cap;
@@ -301,11 +306,22 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.skip_rule = j.skip_rule;
     a.ratio_thr = j.ratio_thr;
     void *args[] = {&a};
-    CK(cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args,
-                        k.dyn_smem, ctx->st));
+    RK(ctx_launch(ctx, k, grid, args));
   }
   ctx->launches++;
   return SETOPS_OK;
+}
+
+// Launches kernel k with one argument block; errors name the launch shape.
+int ctx_launch(setops_ctx *ctx, const KernelInfo &k, uint64_t grid,
+               void **args) {
+  const cudaError_t e = cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt),
+                                         args, k.dyn_smem, ctx->st);
+  if (e == cudaSuccess) return SETOPS_OK;
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "launch of %s (grid %llu, block %d, %zu B shared)",
+                k.name, (unsigned long long)grid, k.nt, k.dyn_smem);
+  return ctx_cuda(ctx, e, buf);
 }
 
 // Copies host arrays into staging slot `slot` and returns the device pointer.

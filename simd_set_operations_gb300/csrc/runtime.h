@@ -90,5 +90,7 @@ setops::Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb,
                           bool bsr, unsigned flags);
 uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr);
 int ctx_launch_pair(setops_ctx *ctx, const setops::PairJob &j);
+int ctx_launch(setops_ctx *ctx, const setops::KernelInfo &k, uint64_t grid,
+               void **args);
 int ctx_stage_in(setops_ctx *ctx, int slot, const uint32_t *h, size_t n,
                  const uint32_t **d);
