@@ -35,17 +35,17 @@ KernelInfo mk_gallop(const char *name) {
 // NT threads; NS slots of C-element chunks per input; window tables of BM
 // words per set (bitmaps of 32*BM values, or BM BSR states)
 const KernelInfo kMergeU32[][2] = {
-    MERGE_ROW(256, 2048, 3, 2048, false),  // 0: 64 KB, 3 CTAs/SM
-    MERGE_ROW(256, 2048, 4, 2048, false),  // 1: 80 KB, deeper prefetch
-    MERGE_ROW(256, 1024, 4, 2048, false),  // 2: 48 KB, 4 CTAs/SM
-    MERGE_ROW(512, 2048, 3, 4096, false),  // 3: wide windows, 16 warps
-    MERGE_ROW(256, 4096, 2, 2048, false),  // 4: big chunks
-    MERGE_ROW(128, 1024, 4, 1024, false),  // 5: 40 KB, 4 warps
+    MERGE_ROW(256, 2048, 2, 4096, false),  // 0: 64 KB, 3 CTAs/SM, W = 2^17
+    MERGE_ROW(256, 2048, 3, 4096, false),  // 1: 80 KB, 2 CTAs/SM
+    MERGE_ROW(256, 2048, 3, 8192, false),  // 2: 112 KB, W = 2^18
+    MERGE_ROW(512, 2048, 3, 8192, false),  // 3: 112 KB, 16 warps
+    MERGE_ROW(256, 1024, 4, 2048, false),  // 4: 48 KB, 4 CTAs/SM
+    MERGE_ROW(256, 2048, 3, 2048, false),  // 5: 64 KB, W = 2^16
 };
 const KernelInfo kMergeBsr[][2] = {
     MERGE_ROW(256, 1024, 3, 2048, true),  // 0: 64 KB
     MERGE_ROW(256, 2048, 2, 2048, true),  // 1: 80 KB
-    MERGE_ROW(128, 1024, 3, 1024, true),  // 2: 56 KB
+    MERGE_ROW(256, 1024, 2, 4096, true),  // 2: 64 KB, wide windows
 };
 // GS lanes per element (1 = thread per element with IT interleaved
 // searches); NS = shared-memory sample of the CTA's bracket (0 = none)

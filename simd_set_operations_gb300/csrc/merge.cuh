@@ -57,6 +57,7 @@ struct MergeArgs {
   uint64_t *out_len;  // device: element count (count / array), or word count
                       // (BSR materialise)
   uint64_t *status;   // look-back words, >= gridDim.x entries
+  uint64_t *coranks;  // per-CTA end co-ranks (epoch-tagged), >= gridDim.x
   LaunchSync *sync;
   int *err;
   uint32_t epoch;
@@ -160,75 +161,71 @@ __device__ __forceinline__ void issue_chunk(const Stream &x, uint32_t c,
   }
 }
 
-// Merge-path co-ranks of two diagonals at once: threads [0, NT/2) search
-// d0, threads [NT/2, NT) search d1, each probing 2 points per round
-// ((NT+1)-ary narrowing; 3 rounds for 2^24-element inputs).  The co-rank of
-// diagonal d is the smallest i with A[i] > B[d-1-i] (A first on ties).
+// Merge-path co-rank of diagonal d: the smallest i with A[i] > B[d-1-i]
+// (A first on ties).  All NT threads cooperate.  Round 1 probes exponentially
+// spaced points around the proportional estimate d*na/(na+nb) (exact for
+// evenly spread values, close for most data), so the later (NT+1)-ary rounds
+// narrow a small bracket whose probes stay in a few DRAM pages.
 template <int NT>
-__device__ __forceinline__ void corank_pair(const uint32_t *A, uint64_t na,
-                                            const uint32_t *B, uint64_t nb,
-                                            uint64_t d0, uint64_t d1,
-                                            uint64_t *i0, uint64_t *i1) {
-  constexpr int H = NT / 2;
-  constexpr uint64_t F = 2 * H + 1;  // fan-out per round
-  __shared__ uint32_t cnt[2];
+__device__ __forceinline__ uint64_t corank_search(const uint32_t *A,
+                                                  uint64_t na,
+                                                  const uint32_t *B,
+                                                  uint64_t nb, uint64_t d) {
+  __shared__ unsigned long long s_lo, s_hi;
   const int t = threadIdx.x;
-  const int half = t >= H;
-  const uint32_t ti = uint32_t(t - half * H);
-  const uint64_t d = half ? d1 : d0;
   uint64_t lo = d > nb ? d - nb : 0;
-  uint64_t hi = d < na ? d : na;
-  for (;;) {
+  uint64_t hi = d < na ? d : na;  // answer in [lo, hi]
+  if (hi - lo > uint64_t(NT)) {
     if (t == 0) {
-      cnt[0] = 0;
-      cnt[1] = 0;
+      s_lo = lo;
+      s_hi = hi;
     }
     __syncthreads();
-    const uint64_t span = hi - lo;
-    uint32_t pr = 0;
-    if (span > 0) {
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const uint64_t k = uint64_t(2 * ti + j);
-        uint64_t x;
-        bool ok;
-        if (span < F) {
-          x = lo + k;
-          ok = k < span;
-        } else {
-          x = lo + ((k + 1) * span) / F;
-          ok = true;
-        }
-        if (ok && __ldg(A + x) <= __ldg(B + (d - 1 - x))) ++pr;
-      }
-    }
-    const unsigned bal1 = __ballot_sync(0xffffffffu, pr >= 1);
-    const unsigned bal2 = __ballot_sync(0xffffffffu, pr >= 2);
-    if ((t & 31) == 0 && (bal1 | bal2))
-      atomicAdd(&cnt[half], __popc(bal1) + __popc(bal2));
-    __syncthreads();
-    const uint64_t c = cnt[half];
-    if (span > 0) {
-      if (span < F) {
-        lo += c;
-        hi = lo;
+    uint64_t est = uint64_t(double(d) * double(na) / double(na + nb));
+    if (est < lo) est = lo;
+    if (est >= hi) est = hi - 1;
+    // probes est + (2^k - 1) and est - 2^k, k = 0..47
+    if (t < 96) {
+      const int k = t % 48;
+      const uint64_t off = (k >= 47) ? (uint64_t(1) << 47) : (uint64_t(1) << k);
+      bool ok;
+      uint64_t x;
+      if (t < 48) {
+        x = est + off - 1;
+        ok = x < hi && x >= est;
       } else {
-        const uint64_t nhi = (c < F - 1) ? lo + ((c + 1) * span) / F : hi;
-        if (c > 0) lo = lo + (c * span) / F + 1;
-        hi = nhi;
+        x = est - off;
+        ok = est >= lo + off;
+      }
+      if (ok) {
+        if (__ldg(A + x) <= __ldg(B + (d - 1 - x))) atomicMax(&s_lo, x + 1);
+        else atomicMin(&s_hi, x);
       }
     }
-    if (__syncthreads_and(hi == lo)) break;
+    __syncthreads();
+    lo = s_lo;
+    hi = s_hi;
+    __syncthreads();
   }
-  *i0 = half ? 0 : lo;
-  *i1 = half ? lo : 0;
-  // broadcast each half's answer to the whole block
-  __shared__ unsigned long long res[2];
-  if (t == 0) res[0] = lo;
-  if (t == H) res[1] = lo;
-  __syncthreads();
-  *i0 = res[0];
-  *i1 = res[1];
+  while (hi > lo) {
+    const uint64_t span = hi - lo;
+    if (span <= uint64_t(NT)) {
+      bool pr = false;
+      if (uint64_t(t) < span) {
+        const uint64_t x = lo + t;
+        pr = __ldg(A + x) <= __ldg(B + (d - 1 - x));
+      }
+      lo += uint64_t(__syncthreads_count(pr));
+      break;
+    }
+    const uint64_t x = lo + (uint64_t(t + 1) * span) / (NT + 1);
+    const uint64_t c =
+        uint64_t(__syncthreads_count(__ldg(A + x) <= __ldg(B + (d - 1 - x))));
+    const uint64_t nhi = (c < uint64_t(NT)) ? lo + ((c + 1) * span) / (NT + 1) : hi;
+    if (c > 0) lo = lo + (c * span) / (NT + 1) + 1;
+    hi = nhi;
+  }
+  return lo;
 }
 
 // Occupancy target for register allocation: the shared-memory footprint
@@ -247,8 +244,6 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
     merge_kernel(const MergeArgs p) {
   using Cfg = MergeCfg<NT, C, NS, BMW, BSR, MAT>;
   constexpr uint32_t WIN = Cfg::kWindow;
-  constexpr int GPC = C / 4;          // 16-byte groups per chunk
-  constexpr int WPT = BMW / NT;       // table words per thread (AND phase)
 
   extern __shared__ __align__(128) uint32_t smem[];
   uint32_t *slotA = smem;
@@ -262,7 +257,7 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
   __shared__ __align__(8) uint64_t barB[NS];
   __shared__ uint32_t warp_sums[NT / 32];
   __shared__ uint32_t s_vid;
-  __shared__ uint32_t s_bound[3];  // by pass, triple-buffered
+  __shared__ uint32_t s_bound[6];  // [pass % 3][stream], triple-buffered
   __shared__ unsigned long long red[NT / 32];
   __shared__ unsigned long long s_excl;
   __shared__ uint32_t s_edge[4];
@@ -300,8 +295,34 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
   const uint64_t d1 = (d0 + D < total) ? d0 + D : total;
 
   // ---- 1. this CTA's runs: A[ia0, ia1) and B[ib0, ib1] ----
-  uint64_t ia0, ia1;
-  corank_pair<NT>(A, na, B, nb, d0, d1, &ia0, &ia1);
+  // Each CTA searches the co-rank of its end diagonal and publishes it; its
+  // start is its predecessor's end (CTA ids come from an atomic ticket, so
+  // the predecessor is running or done).
+  const uint64_t ia1 = corank_search<NT>(A, na, B, nb, d1);
+  __shared__ unsigned long long s_ia0;
+  if (t == 0) {
+    st_release_u64(&p.coranks[vid], pack_status(p.epoch, kFlagPrefix, ia1));
+    uint64_t v0 = 0;
+    if (vid > 0) {
+      const uint64_t t0 = global_ns();
+      for (;;) {
+        const uint64_t w = ld_acquire_u64(&p.coranks[vid - 1]);
+        if (uint32_t(w >> 48) == (p.epoch & 0xffffu) && ((w >> 46) & 3) == kFlagPrefix) {
+          v0 = w & kValueMask;
+          break;
+        }
+        if (global_ns() - t0 > kWaitLimitNs) {
+          record_error(p.err, DEV_ERR_TIMEOUT_LOOKBACK);
+          v0 = UINT64_MAX;
+          break;
+        }
+      }
+    }
+    s_ia0 = v0;
+  }
+  __syncthreads();
+  if (s_ia0 == UINT64_MAX) return;  // error recorded; the host resets state
+  const uint64_t ia0 = s_ia0;
   const uint64_t ib0 = d0 - ia0;
   const uint64_t ib1 = d1 - ia1;
   // B[ib1] is the one element past the range that can match A[ia1-1]
@@ -375,7 +396,9 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
       // ================= dense: value windows =================
       // Per stream: current chunk and cursor (slot index of its first
       // unconsumed element).  Window [w, w + wlen) takes a prefix of what is
-      // left of each stream; w is the smaller of the two cursor values.
+      // left of each stream, w being the smaller of the two cursor values.
+      // One pass inserts from both streams' current chunks (one barrier); a
+      // stream is finished for the window once an element past it is seen.
       if (!wait_chunk(barA, 0) || !wait_chunk(barB, 0)) aborted = true;
       uint32_t qa0, qa1, qb0, qb1;
       qrange(xa, 0, qa0, qa1);
@@ -383,136 +406,171 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
       uint32_t curA = qa0, curB = qb0;
       bool doneA = false, doneB = false;
       uint32_t pass = 0;
-      if (t == 0) {
-        s_bound[0] = 0xffffffffu;
-        s_bound[1] = 0xffffffffu;
-        s_bound[2] = 0xffffffffu;
-      }
+      if (t < 6) s_bound[t] = 0xffffffffu;
       __syncthreads();
+      constexpr int NWP = NT / 32;        // warps
+      constexpr int WPW = BMW / NWP;      // table words per warp
+      constexpr int KW = WPW / 32;        // words per lane
+      static_assert(WPW % 32 == 0, "table words per warp must be a multiple of 32");
       while (!aborted) {
         const uint32_t va = slotA[(ca % NS) * C + curA];
         const uint32_t vb = slotB[(cb % NS) * C + curB];
         const uint32_t w = va < vb ? va : vb;
         const uint32_t wlen =
             (uint64_t(w) + WIN > 0x100000000ull) ? uint32_t(0x100000000ull - w) : WIN;
-#pragma unroll 1
-        for (int sidx = 0; sidx < 2 && !aborted; ++sidx) {
-          const bool isA = sidx == 0;
-          const Stream &x = isA ? xa : xb;
-          uint32_t *slots = isA ? slotA : slotB;
-          uint32_t *slots_s = isA ? slotSA : slotSB;
-          uint64_t *bars = isA ? barA : barB;
-          uint32_t *tab = isA ? tabA : tabB;
-          uint32_t &c = isA ? ca : cb;
-          uint32_t &cur = isA ? curA : curB;
-          bool &done = isA ? doneA : doneB;
-          uint32_t &issued = isA ? issuedA : issuedB;
-          for (;;) {
-            const uint32_t *sl = slots + (c % NS) * C;
-            const uint32_t *sls = BSR ? slots_s + (c % NS) * C : nullptr;
+        bool actA = true, actB = true;  // still inserting into this window
+        while (actA || actB) {
+          uint32_t stopA = 0xffffffffu, stopB = 0xffffffffu;
+#pragma unroll
+          for (int sidx = 0; sidx < 2; ++sidx) {
+            const bool isA = sidx == 0;
+            if (!(isA ? actA : actB)) continue;
+            const Stream &x = isA ? xa : xb;
+            const uint32_t c = isA ? ca : cb;
+            const uint32_t cur = isA ? curA : curB;
+            const uint32_t *sl = (isA ? slotA : slotB) + (c % NS) * C;
+            const uint32_t *sls = BSR ? (isA ? slotSA : slotSB) + (c % NS) * C : nullptr;
+            uint32_t *tab = isA ? tabA : tabB;
             uint32_t q0, q1;
             qrange(x, c, q0, q1);
-            // every element from the cursor on is >= w; insert the prefix
-            // below w + wlen, each thread stopping at its first element past it
+            const uint32_t g0 = cur >> 2, g1 = (q1 + 3) >> 2;
             uint32_t stop = 0xffffffffu;
-            const uint32_t g1 = (q1 + 3) >> 2;
-            for (uint32_t g = (cur >> 2) + t; g < g1; g += NT) {
+            for (uint32_t g = g0 + t; g < g1; g += NT) {
               const uint4 v4 = reinterpret_cast<const uint4 *>(sl)[g];
-              const uint32_t vv[4] = {v4.x, v4.y, v4.z, v4.w};
+              const uint32_t qb = 4 * g;
+              const uint32_t o[4] = {v4.x - w, v4.y - w, v4.z - w, v4.w - w};
+              const bool edge = (g == g0) | (g + 1 == g1);
+              uint32_t outm = 0;
 #pragma unroll
               for (int e2 = 0; e2 < 4; ++e2) {
-                const uint32_t q = 4 * g + e2;
-                if (q < cur || q >= q1) continue;
-                const uint32_t o = vv[e2] - w;
-                if (o < wlen) {
-                  if (BSR) tab[o] = sls[q];
-                  else atomicOr(&tab[o >> 5], 1u << (o & 31u));
-                } else if (stop == 0xffffffffu) {
-                  stop = q;
+                const bool valid = !edge || ((qb + e2 >= cur) && (qb + e2 < q1));
+                const bool in = valid && (o[e2] < wlen);
+                if (in) {
+                  if (BSR) tab[o[e2]] = sls[qb + e2];
+                  else atomicOr(&tab[o[e2] >> 5], 1u << (o[e2] & 31u));
                 }
+                outm |= uint32_t(valid && !in) << e2;
               }
-              if (stop != 0xffffffffu) break;
+              if (outm) {
+                stop = qb + uint32_t(__ffs(outm) - 1);
+                break;
+              }
             }
-            const uint32_t wstop = __reduce_min_sync(0xffffffffu, stop);
-            if (lane == 0 && wstop != 0xffffffffu) atomicMin(&s_bound[pass % 3], wstop);
-            __syncthreads();  // chunk reads and s_bound done
-            const uint32_t bnd = s_bound[pass % 3];
-            if (t == 0) s_bound[(pass + 2) % 3] = 0xffffffffu;
-            ++pass;
+            if (isA) stopA = stop;
+            else stopB = stop;
+          }
+          const uint32_t wsa = __reduce_min_sync(0xffffffffu, stopA);
+          const uint32_t wsb = __reduce_min_sync(0xffffffffu, stopB);
+          const uint32_t slot = (pass % 3) * 2;
+          if (lane == 0) {
+            if (wsa != 0xffffffffu) atomicMin(&s_bound[slot], wsa);
+            if (wsb != 0xffffffffu) atomicMin(&s_bound[slot + 1], wsb);
+          }
+          __syncthreads();  // chunk reads and bounds done
+          const uint32_t bA = s_bound[slot], bB = s_bound[slot + 1];
+          if (t < 2) s_bound[((pass + 2) % 3) * 2 + t] = 0xffffffffu;
+          ++pass;
+          bool waitA = false, waitB = false;
+#pragma unroll
+          for (int sidx = 0; sidx < 2; ++sidx) {
+            const bool isA = sidx == 0;
+            bool &act = isA ? actA : actB;
+            if (!act) continue;
+            const uint32_t bnd = isA ? bA : bB;
             if (bnd != 0xffffffffu) {  // the window ends inside this chunk
-              cur = bnd;
-              break;
+              (isA ? curA : curB) = bnd;
+              act = false;
+              continue;
             }
-            refill(x, slots, slots_s, bars, c, issued);
+            const Stream &x = isA ? xa : xb;
+            uint32_t &c = isA ? ca : cb;
+            refill(x, isA ? slotA : slotB, isA ? slotSA : slotSB, isA ? barA : barB,
+                   c, isA ? issuedA : issuedB);
             ++c;
             if (c >= x.nc) {
-              done = true;
-              break;
-            }
-            if (!wait_chunk(bars, c)) {
-              aborted = true;
-              break;
+              (isA ? doneA : doneB) = true;
+              act = false;
+              continue;
             }
             uint32_t n0, n1;
             qrange(x, c, n0, n1);
-            cur = n0;
+            (isA ? curA : curB) = n0;
+            (isA ? waitA : waitB) = true;
+          }
+          if (waitA || waitB) {
+            bool ok = true;
+            if (waitA) ok = mbar_wait_bounded(&barA[ca % NS], (ca / NS) & 1u, p.err);
+            if (ok && waitB) ok = mbar_wait_bounded(&barB[cb % NS], (cb / NS) & 1u, p.err);
+            if (__syncthreads_or(!ok)) {
+              aborted = true;
+              break;
+            }
           }
         }
         if (aborted) break;
-        // AND the two tables and clear them; thread t owns words
-        // [t*WPT, (t+1)*WPT), so matches come out in ascending order
+        // AND the two tables.  Warp wp owns words [wp*WPW, (wp+1)*WPW), lane l
+        // words wp*WPW + 32k + l (conflict-free); word order = value order.
+        const int wp = t >> 5;
+        uint32_t *ta = tabA + wp * WPW + lane;
+        uint32_t *tb = tabB + wp * WPW + lane;
         uint32_t hits = 0;
-        uint32_t myw[WPT];
-#pragma unroll
-        for (int j = 0; j < WPT; j += 4) {
-          uint4 *pa = reinterpret_cast<uint4 *>(tabA + t * WPT) + j / 4;
-          uint4 *pb = reinterpret_cast<uint4 *>(tabB + t * WPT) + j / 4;
-          const uint4 x4 = *pa, y4 = *pb;
-          *pa = make_uint4(0, 0, 0, 0);
-          *pb = make_uint4(0, 0, 0, 0);
-          myw[j] = x4.x & y4.x;
-          myw[j + 1] = x4.y & y4.y;
-          myw[j + 2] = x4.z & y4.z;
-          myw[j + 3] = x4.w & y4.w;
-        }
-#pragma unroll
-        for (int j = 0; j < WPT; ++j) {
+#pragma unroll 4
+        for (int k = 0; k < KW; ++k) {
+          const uint32_t m = ta[32 * k] & tb[32 * k];
+          tb[32 * k] = 0;
+          ta[32 * k] = MAT ? m : 0u;
           if (BSR) {
-            if (MAT) hits += (myw[j] != 0);
-            else cnt += __popc(myw[j]);
+            if (MAT) hits += (m != 0);
+            else cnt += __popc(m);
           } else {
-            hits += __popc(myw[j]);
+            hits += __popc(m);
           }
         }
         if (MAT) {
-          // block scan only for windows that have matches
-          if (__syncthreads_or(hits != 0)) {
-            uint32_t tot;
-            const uint32_t ex = block_exclusive_scan<NT>(hits, warp_sums, &tot);
-            if (hits) {
-              uint32_t *dst = p.stage + stage_base + cta_cnt + ex;
-              uint32_t *dsts = BSR ? p.stage_s + stage_base + cta_cnt + ex : nullptr;
-              uint32_t o = 0;
+          // warp totals -> block offsets (only when the window has matches)
+          uint32_t wt = hits;
 #pragma unroll
-              for (int j = 0; j < WPT; ++j) {
-                uint32_t m = myw[j];
-                const uint32_t wbase = w + uint32_t(t * WPT + j) * (BSR ? 1u : 32u);
-                if (BSR) {
-                  if (m) {
-                    dst[o] = wbase;
-                    dsts[o] = m;
-                    ++o;
-                  }
-                } else {
-                  while (m) {
-                    dst[o++] = wbase + uint32_t(__ffs(m) - 1);
-                    m &= m - 1;
-                  }
+          for (int of = 16; of > 0; of >>= 1) wt += __shfl_xor_sync(0xffffffffu, wt, of);
+          if (__syncthreads_or(hits != 0)) {
+            if (lane == 0) warp_sums[wp] = wt;
+            __syncthreads();
+            uint32_t woff = 0, tot = 0;
+#pragma unroll
+            for (int i = 0; i < NWP; ++i) {
+              const uint32_t v = warp_sums[i];
+              woff += (i < wp) ? v : 0u;
+              tot += v;
+            }
+            uint64_t o = stage_base + cta_cnt + woff;
+            for (int k = 0; k < KW; ++k) {
+              uint32_t m = ta[32 * k];
+              if (!__any_sync(0xffffffffu, m != 0)) continue;
+              ta[32 * k] = 0;
+              const uint32_t pc = BSR ? uint32_t(m != 0) : uint32_t(__popc(m));
+              uint32_t incl = pc;
+#pragma unroll
+              for (int of = 1; of < 32; of <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, of);
+                if (lane >= of) incl += y;
+              }
+              uint64_t q = o + incl - pc;
+              const uint32_t wbase = w + uint32_t(wp * WPW + 32 * k + lane) * (BSR ? 1u : 32u);
+              if (BSR) {
+                if (m) {
+                  p.stage[q] = wbase;
+                  p.stage_s[q] = m;
+                }
+              } else {
+                while (m) {
+                  p.stage[q++] = wbase + uint32_t(__ffs(m) - 1);
+                  m &= m - 1;
                 }
               }
+              o += __shfl_sync(0xffffffffu, incl, 31);
             }
             cta_cnt += tot;
           }
+          // every nonzero AND word was extracted and cleared above
         } else if (!BSR) {
           cnt += hits;
         }

@@ -246,7 +246,9 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   }
   if (j.grid_cap && grid > j.grid_cap) grid = j.grid_cap;
   uint32_t epoch = 0;
-  if (mat) RK(ctx_status_words(ctx, status_words));
+  // merge kernels publish per-CTA co-ranks after the look-back words
+  const bool merge = j.choice.algo == ALGO_MERGE;
+  RK(ctx_status_words(ctx, merge ? status_words + grid : status_words));
   RK(ctx_next_epoch(ctx, &epoch));
   LaunchSync *sync = ctx->sync + j.sync_slot;
 
@@ -276,6 +278,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.out_cap = j.out_cap;
     a.out_len = j.len_dev;
     a.status = static_cast<uint64_t *>(ctx->status.p);
+    a.coranks = static_cast<uint64_t *>(ctx->status.p) + grid;
     a.sync = sync;
     a.err = ctx->derr;
     a.epoch = epoch;
