@@ -74,6 +74,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Non-blocking test: has phase `parity` of `bar` completed?
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Named barrier `ID` over N threads (N a multiple of 32).
+template <int ID, int N>
+__device__ __forceinline__ void named_bar_sync() {
+  asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(N) : "memory");
+}
+
 // Waits for phase `parity` of `bar` to complete.  Returns false (and records
 // DEV_ERR_TIMEOUT_MBAR) if the limit is reached.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
@@ -86,6 +105,26 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   }
   record_error(err, DEV_ERR_TIMEOUT_MBAR);
   return false;
+}
+
+// As mbar_wait_bounded, for blocks whose threads share an abort flag in
+// shared memory: a timeout sets the flag, and a wait that sees the flag set
+// gives up at once, so one failed copy costs one time limit, not one per
+// later wait.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar,
+                                                    uint32_t parity, int *err,
+                                                    volatile uint32_t *abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (global_ns() - t0 > kWaitLimitNs) {
+      record_error(err, DEV_ERR_TIMEOUT_MBAR);
+      *abort = 1u;
+      return false;
+    }
+  }
 }
 
 // 1-D bulk copy global -> shared, completing `bytes` on `bar`.  dst, src and

@@ -9,12 +9,12 @@ namespace setops {
 
 namespace {
 
-template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
+template <int NW, int C, int NSA, int NSB, int VW, bool BSR, bool MAT>
 KernelInfo mk_merge(const char *name) {
+  using Cfg = MergeCfg<NW, C, NSA, NSB, VW, BSR, MAT>;
   return KernelInfo{reinterpret_cast<const void *>(
-                        &merge_kernel<NT, C, NS, BMW, BSR, MAT>),
-                    NT, MergeCfg<NT, C, NS, BMW, BSR, MAT>::kSmemBytes, C,
-                    name};
+                        &merge_kernel<NW, C, NSA, NSB, VW, BSR, MAT>),
+                    Cfg::kThreads, Cfg::kSmemBytes, C, name};
 }
 
 template <int NT, int GS, int ITEMS, int NSAMP, bool BSR, bool MAT>
@@ -25,27 +25,29 @@ KernelInfo mk_gallop(const char *name) {
 }
 
 // [variant][count, materialise]
-#define MERGE_ROW(NT, C, NS, BM, BSR)                                          \
-  {mk_merge<NT, C, NS, BM, BSR, false>("merge_" #NT "_c" #C "x" #NS "_t" #BM), \
-   mk_merge<NT, C, NS, BM, BSR, true>("merge_" #NT "_c" #C "x" #NS "_t" #BM)}
+#define MERGE_ROW(NW, C, NSA, NSB, VW, BSR)                                   \
+  {mk_merge<NW, C, NSA, NSB, VW, BSR, false>(                                 \
+       "merge_w" #NW "_c" #C "_s" #NSA "x" #NSB "_t" #VW),                    \
+   mk_merge<NW, C, NSA, NSB, VW, BSR, true>(                                  \
+       "merge_w" #NW "_c" #C "_s" #NSA "x" #NSB "_t" #VW)}
 #define GALLOP_ROW(NT, GS, IT, NS, BSR)                                         \
   {mk_gallop<NT, GS, IT, NS, BSR, false>("gallop_" #NT "_g" #GS "_i" #IT "_s" #NS), \
    mk_gallop<NT, GS, IT, NS, BSR, true>("gallop_" #NT "_g" #GS "_i" #IT "_s" #NS)}
 
-// NT threads; NS slots of C-element chunks per input; window tables of BM
-// words per set (bitmaps of 32*BM values, or BM BSR states)
+// NW warps; C-element chunks in NSA / NSB slots for A / B; T buffers of VW
+// words (bitmaps of 32*VW values, or VW BSR states)
 const KernelInfo kMergeU32[][2] = {
-    MERGE_ROW(256, 2048, 2, 4096, false),  // 0: 64 KB, 3 CTAs/SM, W = 2^17
-    MERGE_ROW(256, 2048, 3, 4096, false),  // 1: 80 KB, 2 CTAs/SM
-    MERGE_ROW(256, 2048, 3, 8192, false),  // 2: 112 KB, W = 2^18
-    MERGE_ROW(512, 2048, 3, 8192, false),  // 3: 112 KB, 16 warps
-    MERGE_ROW(256, 1024, 4, 2048, false),  // 4: 48 KB, 4 CTAs/SM
-    MERGE_ROW(256, 2048, 3, 2048, false),  // 5: 64 KB, W = 2^16
+    MERGE_ROW(8, 2048, 2, 3, 2048, false),   // 0: 64 KB, 3 CTAs/SM
+    MERGE_ROW(8, 2048, 3, 3, 2048, false),   // 1: 72 KB, 3 CTAs/SM
+    MERGE_ROW(4, 2048, 2, 3, 2048, false),   // 2: 4 warps
+    MERGE_ROW(8, 2048, 3, 4, 2048, false),   // 3: 80 KB, 2 CTAs/SM
+    MERGE_ROW(4, 1024, 2, 4, 1024, false),   // 4: 36 KB, 5 CTAs/SM
+    MERGE_ROW(8, 1024, 3, 4, 2048, false),   // 5: 52 KB, 4 CTAs/SM
 };
 const KernelInfo kMergeBsr[][2] = {
-    MERGE_ROW(256, 1024, 3, 2048, true),  // 0: 64 KB
-    MERGE_ROW(256, 2048, 2, 2048, true),  // 1: 80 KB
-    MERGE_ROW(256, 1024, 2, 4096, true),  // 2: 64 KB, wide windows
+    MERGE_ROW(8, 1024, 2, 3, 2048, true),  // 0: 56 KB
+    MERGE_ROW(8, 2048, 2, 2, 4096, true),  // 1: 96 KB
+    MERGE_ROW(8, 1024, 2, 2, 4096, true),  // 2: 64 KB
 };
 // GS lanes per element (1 = thread per element with IT interleaved
 // searches); NS = shared-memory sample of the CTA's bracket (0 = none)

@@ -9,32 +9,44 @@
 // Work layout
 // -----------
 // Let A be the smaller input.  The merged sequence (A first on ties; length
-// na+nb) is cut into one contiguous diagonal range per CTA, whose merge-path
-// co-ranks (both ends) one block search finds.  The CTA owns A[ia0, ia1) and
-// reads B[ib0, ib1] -- B[ib1] is the one element past the range that can
-// equal the CTA's last A element; a match is counted by the CTA owning its A
-// element, so every match is counted once.
+// na+nb) is cut into one contiguous diagonal range per CTA; each CTA finds
+// the merge-path co-rank of its end diagonal and takes its start from its
+// predecessor.  The CTA owns A[ia0, ia1) and reads B[ib0, ib1] -- B[ib1] is
+// the one element past the range that can equal the CTA's last A element; a
+// match is counted by the CTA owning its A element, so every match is
+// counted once.
 //
-// The two runs stream independently through shared memory: fixed chunks of
-// C elements, 16-byte aligned, loaded by 1-D TMA bulk copies into NS slots
-// per stream, each slot with its own mbarrier; a slot is refilled as soon as
-// its chunk is used up.
+// Streaming.  Both runs flow through shared memory in fixed chunks of C
+// elements (16-byte aligned 1-D TMA bulk copies) into NSA / NSB slots.  Each
+// slot has an mbarrier completed by the copy's byte count and a release
+// counter: every warp adds one when it is done with the slot's chunk, and
+// the warp that completes the count issues the copy of the chunk NS places
+// later into the same slot.  Warps therefore never stop at a block-wide
+// barrier between chunks, and no thread polls for free slots.
 //
-// Dense runs (at least one element per 64 values) are intersected in value
-// windows: every element of window [w, w + 32*BMW) sets its bit in its
-// set's window bitmap (atomicOr; for BSR the state word is stored at its
-// base), the two tables are AND-ed word by word, and the set bits are the
-// matches, already in ascending order (one block scan per window orders the
-// output).  The next window starts at the smallest value not yet consumed,
-// so empty value ranges are skipped.  Sparse runs are intersected chunk pair
-// by chunk pair (binary search of each A element in the B chunk, advancing
-// the chunk with the smaller maximum, as in the reference's block-wise SIMD
-// algorithms, setops/src/intersect/shuffling.rs:69-112).
+// Dense runs (A holds at least one element per 64 values; BSR: per 2 bases)
+// are intersected group by group.  A group is a run of consecutive A
+// elements of one chunk whose values span less than kSpan.  Its elements set
+// their bits in bitmap T (BSR: their state words at their base); then every
+// B element in the group's value range probes T.  Matches set their bit in
+// bitmap M (indexed by value, so M is in ascending order); after the group
+// one warp (a different one each group) writes M's set bits to the output in
+// order.  Two T buffers alternate, so the next group's insertion and the last
+// group's extraction and clearing share one phase: two barriers per group.
+// A B chunk whose last value does not exceed the group's last value is
+// released; otherwise the group ends and the chunk's remaining elements
+// (found by a binary search for the group's last value) go to the next group.
+//
+// Sparse runs are intersected chunk pair by chunk pair (binary search of each
+// A element in the B chunk, advancing the chunk with the smaller maximum, as
+// in the reference's block-wise SIMD algorithms, setops/src/intersect/
+// shuffling.rs:69-112).
 //
 // Count mode adds per-CTA totals atomically; the last CTA writes the total.
 // Materialise mode stages a CTA's matches in scratch at its first A index
 // (an exclusive region: a CTA cannot emit more matches than A elements it
-// owns); decoupled look-back over CTAs gives each CTA its output offset.
+// owns); each CTA sums its predecessors' published match counts to get its
+// output offset.
 #pragma once
 
 #include "common.cuh"
@@ -56,7 +68,7 @@ struct MergeArgs {
   uint64_t out_cap;
   uint64_t *out_len;  // device: element count (count / array), or word count
                       // (BSR materialise)
-  uint64_t *status;   // look-back words, >= gridDim.x entries
+  uint64_t *status;   // per-CTA count words, >= gridDim.x entries
   uint64_t *coranks;  // per-CTA end co-ranks (epoch-tagged), >= gridDim.x
   LaunchSync *sync;
   int *err;
@@ -68,19 +80,27 @@ struct MergeArgs {
   uint32_t ratio_thr;
 };
 
-// Shapes: NT threads, chunks of C elements per stream, NS chunk slots per
-// stream, window tables of BMW words per set.
-template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
+// Shapes: NW warps; chunks of C elements; NSA / NSB chunk slots for A / B;
+// T buffers of VW words (arrays: one bit per value, so a group spans
+// < 32*VW values; BSR: one state word per base).
+template <int NW, int C, int NSA, int NSB, int VW, bool BSR, bool MAT>
 struct MergeCfg {
-  static_assert(C % (4 * NT) == 0 || (4 * NT) % C == 0, "chunk / block shape");
-  static_assert(C % 4 == 0 && BMW % (4 * NT) == 0, "16-byte groups");
-  static_assert(NS >= 2, "need at least double buffering");
-  static constexpr int kSlotWords = NS * C;                    // per stream
-  static constexpr int kStreams = BSR ? 4 : 2;                 // keys (+ states)
+  static constexpr int kThreads = NW * 32;
+  static_assert(C % 4 == 0 && VW % (4 * NW) == 0, "16-byte groups");
+  static_assert(NSA >= 2 && NSB >= 2, "need at least double buffering");
+  static_assert((VW & (VW - 1)) == 0, "power-of-two table");
+  static constexpr uint32_t kSpan = BSR ? uint32_t(VW) : uint32_t(VW) * 32u;
+  // T buffer: VW words plus a zero pad word group, so a probe can clamp an
+  // out-of-range offset to the group's span + 1 and read a zero bit there
+  static constexpr int kTabWords = VW + 4;
+  // match bitmap M: one bit per value (arrays) or per base (BSR), and its
+  // summary: one bit per nonzero M word
+  static constexpr int kMWords = MAT ? int((kSpan / 32 + 1023) & ~1023u) : 0;
+  static constexpr int kSumWords = kMWords / 32;
+  static constexpr int kStreams = BSR ? 2 : 1;  // keys (+ states) per input
+  static constexpr size_t kSlotWords = size_t(NSA + NSB) * C * kStreams;
   static constexpr size_t kSmemBytes =
-      (size_t(kStreams) * kSlotWords + 2 * size_t(BMW)) * 4;
-  // values (arrays: one bit each) or bases (BSR: one state word each) per window
-  static constexpr uint32_t kWindow = BSR ? uint32_t(BMW) : uint32_t(BMW) * 32u;
+      (kSlotWords + 2 * size_t(kTabWords) + size_t(kMWords) + size_t(kSumWords)) * 4;
   static constexpr int kTile = C;  // elements per chunk, for grid sizing
 };
 
@@ -228,42 +248,126 @@ __device__ __forceinline__ uint64_t corank_search(const uint32_t *A,
   return lo;
 }
 
+// Exclusive scan of one uint32 per thread, synchronising on named barrier 1
+// (all NT threads).  `warp_sums` needs NT/32 entries; the caller must pass
+// another barrier before the next call.
+template <int NT>
+__device__ __forceinline__ uint32_t scan_exclusive_nb(uint32_t v,
+                                                      uint32_t *warp_sums,
+                                                      uint32_t *total) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  named_bar_sync<1, NT>();
+  uint32_t wpre = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const uint32_t s = warp_sums[w];
+    wpre += (w < warp) ? s : 0u;
+    tot += s;
+  }
+  *total = tot;
+  return wpre + x - v;
+}
+
+// Exclusive prefix of per-CTA counts, for blocks whose CTA ids come from an
+// atomic ticket (so every predecessor is running or done).  The CTA
+// publishes its own count (epoch-tagged), then all threads sum the published
+// counts of every predecessor at once: one or two rounds of loads however
+// many CTAs precede it, where a chained look-back needs one round per 32
+// predecessors when all CTAs finish together.  All NT threads (named
+// barrier 1); returns UINT64_MAX after recording a timeout.
+template <int NT>
+__device__ __forceinline__ uint64_t predecessor_sum(uint64_t *status,
+                                                    uint32_t vid,
+                                                    uint64_t count,
+                                                    uint32_t epoch, int *err,
+                                                    unsigned long long *red) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) st_release_u64(&status[vid], pack_status(epoch, kFlagAggregate, count));
+  const uint32_t ep = epoch & 0xffffu;
+  uint64_t sum = 0;
+  bool bad = false;
+  for (uint32_t j = uint32_t(t); j < vid && !bad; j += NT) {
+    uint64_t w = ld_acquire_u64(&status[j]);
+    if (uint32_t(w >> 48) != ep) {
+      const uint64_t t0 = global_ns();
+      do {
+        if (global_ns() - t0 > kWaitLimitNs) {
+          record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
+          bad = true;
+          break;
+        }
+        w = ld_acquire_u64(&status[j]);
+      } while (uint32_t(w >> 48) != ep);
+    }
+    sum += w & kValueMask;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  const bool any_bad = __any_sync(0xffffffffu, bad);
+  if (lane == 0) red[warp] = any_bad ? ~0ull : sum;
+  named_bar_sync<1, NT>();
+  uint64_t tot = 0;
+  bool fail = false;
+#pragma unroll
+  for (int w = 0; w < NT / 32; ++w) {
+    const unsigned long long v = red[w];
+    fail |= (v == ~0ull);
+    tot += v;
+  }
+  return fail ? UINT64_MAX : tot;
+}
+
 // Occupancy target for register allocation: the shared-memory footprint
 // allows at most this many CTAs per SM anyway.
-template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
+template <int NW, int C, int NSA, int NSB, int VW, bool BSR, bool MAT>
 constexpr int merge_min_blocks() {
-  constexpr size_t smem = MergeCfg<NT, C, NS, BMW, BSR, MAT>::kSmemBytes + 1024;
+  using Cfg = MergeCfg<NW, C, NSA, NSB, VW, BSR, MAT>;
+  constexpr size_t smem = Cfg::kSmemBytes + 2048;
   constexpr int by_smem = int((228 * 1024) / smem);
-  constexpr int by_threads = 2048 / NT;
+  constexpr int by_threads = 2048 / Cfg::kThreads;
   constexpr int b = by_smem < by_threads ? by_smem : by_threads;
   return b < 1 ? 1 : b;
 }
 
-template <int NT, int C, int NS, int BMW, bool BSR, bool MAT>
-__global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT>()))
+template <int NW, int C, int NSA, int NSB, int VW, bool BSR, bool MAT>
+__global__ void __launch_bounds__(
+    MergeCfg<NW, C, NSA, NSB, VW, BSR, MAT>::kThreads,
+    (merge_min_blocks<NW, C, NSA, NSB, VW, BSR, MAT>()))
     merge_kernel(const MergeArgs p) {
-  using Cfg = MergeCfg<NT, C, NS, BMW, BSR, MAT>;
-  constexpr uint32_t WIN = Cfg::kWindow;
+  using Cfg = MergeCfg<NW, C, NSA, NSB, VW, BSR, MAT>;
+  constexpr int NT = Cfg::kThreads;
+  constexpr uint32_t SPAN = Cfg::kSpan;
+  constexpr uint32_t TW = uint32_t(Cfg::kTabWords);
 
   extern __shared__ __align__(128) uint32_t smem[];
-  uint32_t *slotA = smem;
-  uint32_t *slotB = smem + Cfg::kSlotWords;
-  uint32_t *slotSA = BSR ? smem + 2 * Cfg::kSlotWords : nullptr;
-  uint32_t *slotSB = BSR ? smem + 3 * Cfg::kSlotWords : nullptr;
-  uint32_t *tabA = smem + Cfg::kStreams * Cfg::kSlotWords;
-  uint32_t *tabB = tabA + BMW;
+  uint32_t *slotA = smem;            // NSA chunks
+  uint32_t *slotB = smem + NSA * C;  // NSB chunks
+  uint32_t *slotSA = BSR ? smem + (NSA + NSB) * C : nullptr;
+  uint32_t *slotSB = BSR ? slotSA + NSA * C : nullptr;
+  uint32_t *tab = smem + Cfg::kSlotWords;  // two T buffers of TW words
+  uint32_t *mbits = tab + 2 * TW;          // match bitmap (materialise)
+  uint32_t *msum = mbits + Cfg::kMWords;   // its nonzero-word summary
 
-  __shared__ __align__(8) uint64_t barA[NS];
-  __shared__ __align__(8) uint64_t barB[NS];
-  __shared__ uint32_t warp_sums[NT / 32];
-  __shared__ uint32_t s_vid;
-  __shared__ uint32_t s_bound[6];  // [pass % 3][stream], triple-buffered
-  __shared__ unsigned long long red[NT / 32];
-  __shared__ unsigned long long s_excl;
-  __shared__ uint32_t s_edge[4];
+  __shared__ __align__(8) uint64_t fullA[NSA], fullB[NSB];
+  __shared__ uint32_t relA[NSA], relB[NSB];    // warps done with the chunk
+  __shared__ uint32_t lastA[NSA], lastB[NSB];  // last chunk issued + 1
+  __shared__ uint32_t warp_sums[NW];
+  __shared__ unsigned long long red[NW];
+  __shared__ unsigned long long s_ia0, s_cnt;
+  __shared__ uint32_t s_vid, s_abort;
+  __shared__ uint32_t s_edge[2];
 
   const int t = threadIdx.x;
   const int lane = t & 31;
+  const int warp = t >> 5;
 
   // ---- problem (A = smaller set) ----
   uint64_t na = p.na_dev ? *p.na_dev : p.na;
@@ -279,13 +383,16 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
 
   if (t == 0) {
     s_vid = atomicAdd(&p.sync->ticket, 1u);
-    for (int i = 0; i < NS; ++i) {
-      mbar_init(&barA[i], 1);
-      mbar_init(&barB[i], 1);
-    }
+    for (int i = 0; i < NSA; ++i) mbar_init(&fullA[i], 1);
+    for (int i = 0; i < NSB; ++i) mbar_init(&fullB[i], 1);
+    s_abort = 0;
+    s_cnt = 0;
     fence_mbar_init();
   }
-  for (int i = t; i < 2 * BMW; i += NT) tabA[i] = 0;  // tabA and tabB
+  if (t < NSA) { relA[t] = 0; lastA[t] = 0; }
+  if (t < NSB) { relB[t] = 0; lastB[t] = 0; }
+  for (int i = t; i < int(2 * TW + Cfg::kMWords + Cfg::kSumWords) / 4; i += NT)
+    reinterpret_cast<uint4 *>(tab)[i] = make_uint4(0, 0, 0, 0);
   __syncthreads();
   const uint32_t vid = s_vid;
   const uint32_t G = gridDim.x;
@@ -299,7 +406,6 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
   // start is its predecessor's end (CTA ids come from an atomic ticket, so
   // the predecessor is running or done).
   const uint64_t ia1 = corank_search<NT>(A, na, B, nb, d1);
-  __shared__ unsigned long long s_ia0;
   if (t == 0) {
     st_release_u64(&p.coranks[vid], pack_status(p.epoch, kFlagPrefix, ia1));
     uint64_t v0 = 0;
@@ -328,35 +434,12 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
   // B[ib1] is the one element past the range that can match A[ia1-1]
   const uint64_t be = ib1 < nb ? ib1 + 1 : nb;
   const uint64_t stage_base = ia0;  // matches <= owned A elements
+  const uint64_t cap = ia1 > ia0 ? ia1 - ia0 : 0;
   const bool work = ia1 > ia0 && be > ib0;
-
+  const Stream xa = make_stream<C>(A, BSR ? SA : nullptr, na, ia0, work ? ia1 : ia0);
+  const Stream xb = make_stream<C>(B, BSR ? SB : nullptr, nb, ib0, work ? be : ib0);
+  volatile uint32_t *abortp = &s_abort;
   const uint64_t pol = l2_evict_first_policy();
-  Stream xa = make_stream<C>(A, BSR ? SA : nullptr, na, ia0, work ? ia1 : ia0);
-  Stream xb = make_stream<C>(B, BSR ? SB : nullptr, nb, ib0, work ? be : ib0);
-  uint32_t issuedA = 0, issuedB = 0;  // chunks issued (thread 0's view)
-  if (t == 0) {
-    for (; issuedA < xa.nc && issuedA < uint32_t(NS); ++issuedA)
-      issue_chunk<C>(xa, issuedA, slotA + (issuedA % NS) * C,
-                     BSR ? slotSA + (issuedA % NS) * C : nullptr,
-                     &barA[issuedA % NS], pol);
-    for (; issuedB < xb.nc && issuedB < uint32_t(NS); ++issuedB)
-      issue_chunk<C>(xb, issuedB, slotB + (issuedB % NS) * C,
-                     BSR ? slotSB + (issuedB % NS) * C : nullptr,
-                     &barB[issuedB % NS], pol);
-    // first / last values of both runs decide dense vs sparse handling
-    if (work) {
-      s_edge[0] = __ldg(A + ia0);
-      s_edge[1] = __ldg(A + ia1 - 1);
-      s_edge[2] = __ldg(B + ib0);
-      s_edge[3] = __ldg(B + be - 1);
-    }
-  }
-  __syncthreads();
-
-  uint32_t ca = 0, cb = 0;  // current chunk of each stream
-  bool aborted = false;
-  uint64_t cnt = 0;      // count mode (BSR: elements)
-  uint64_t cta_cnt = 0;  // materialise: matches staged so far
 
   // Valid slot-index range of chunk c of stream x.
   auto qrange = [&](const Stream &x, uint32_t c, uint32_t &q0, uint32_t &q1) {
@@ -365,235 +448,307 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
     q0 = vs > cs ? uint32_t(vs - cs) : 0u;
     q1 = ve < cs + C ? uint32_t(ve - cs) : uint32_t(C);
   };
-  // Waits (all threads) for chunk c of a stream; false on timeout.
-  auto wait_chunk = [&](uint64_t *bars, uint32_t c) -> bool {
-    const bool ok = mbar_wait_bounded(&bars[c % NS], (c / NS) & 1u, p.err);
-    return !__syncthreads_or(!ok);
+  // This warp is done with chunk c of A (B): the last warp to say so loads
+  // chunk c + NS into the slot.  Call with the whole warp.
+  auto release_a = [&](uint32_t c) {
+    __syncwarp();
+    if (lane == 0) {
+      const uint32_t s = c % NSA;
+      __threadfence_block();
+      if (atomicAdd(&relA[s], 1u) == uint32_t(NW - 1)) {
+        relA[s] = 0;
+        __threadfence_block();
+        const uint32_t nx = c + NSA;
+        if (nx < xa.nc) {
+          issue_chunk<C>(xa, nx, slotA + s * C, BSR ? slotSA + s * C : nullptr, &fullA[s], pol);
+          lastA[s] = nx + 1;
+        }
+      }
+    }
   };
-  // Releases chunk c's slot (call after a barrier) and loads chunk c + NS.
-  auto refill = [&](const Stream &x, uint32_t *slots, uint32_t *slots_s,
-                    uint64_t *bars, uint32_t c, uint32_t &issued) {
-    if (t == 0 && c + NS < x.nc) {
-      const uint32_t nx = c + NS;
-      issue_chunk<C>(x, nx, slots + (nx % NS) * C,
-                     BSR ? slots_s + (nx % NS) * C : nullptr, &bars[nx % NS],
-                     pol);
-      issued = nx + 1;
+  auto release_b = [&](uint32_t c) {
+    __syncwarp();
+    if (lane == 0) {
+      const uint32_t s = c % NSB;
+      __threadfence_block();
+      if (atomicAdd(&relB[s], 1u) == uint32_t(NW - 1)) {
+        relB[s] = 0;
+        __threadfence_block();
+        const uint32_t nx = c + NSB;
+        if (nx < xb.nc) {
+          issue_chunk<C>(xb, nx, slotB + s * C, BSR ? slotSB + s * C : nullptr, &fullB[s], pol);
+          lastB[s] = nx + 1;
+        }
+      }
     }
   };
 
+  uint32_t cnt = 0;      // count mode (BSR: elements)
+  uint64_t cta_cnt = 0;  // materialise: matches staged
+
   if (work) {
-    const uint32_t a_first = s_edge[0], a_last = s_edge[1];
-    const uint32_t b_first = s_edge[2], b_last = s_edge[3];
-    const uint32_t vmin = a_first < b_first ? a_first : b_first;
-    const uint32_t vmax = a_last > b_last ? a_last : b_last;
-    const uint64_t elems = (ia1 - ia0) + (be - ib0);
-    // dense when a window table pays for itself: at least one element per
-    // 64 values (arrays) / per 2 bases (BSR) over the run's value span
-    const bool dense = BSR ? (2 * elems >= uint64_t(vmax - vmin) + 1)
-                           : (64 * elems >= uint64_t(vmax - vmin) + 1);
+    if (t == 0) {
+      for (uint32_t c = 0; c < xa.nc && c < uint32_t(NSA); ++c) {
+        issue_chunk<C>(xa, c, slotA + c * C, BSR ? slotSA + c * C : nullptr, &fullA[c], pol);
+        lastA[c] = c + 1;
+      }
+      for (uint32_t c = 0; c < xb.nc && c < uint32_t(NSB); ++c) {
+        issue_chunk<C>(xb, c, slotB + c * C, BSR ? slotSB + c * C : nullptr, &fullB[c], pol);
+        lastB[c] = c + 1;
+      }
+      s_edge[0] = __ldg(A + ia0);
+      s_edge[1] = __ldg(A + ia1 - 1);
+    }
+    __syncthreads();
+    const uint64_t aspan = uint64_t(s_edge[1] - s_edge[0]) + 1;
+    // groups pay for themselves when A holds at least one element per 64
+    // values (arrays) / per 2 bases (BSR)
+    const bool dense = BSR ? (2 * cap >= aspan) : (64 * cap >= aspan);
+    uint32_t ca = 0, cb = 0;  // current chunk of each stream
+    uint32_t qa0, qa1, qb0, qb1;
+    qrange(xa, 0, qa0, qa1);
+
     if (dense) {
-      // ================= dense: value windows =================
-      // Per stream: current chunk and cursor (slot index of its first
-      // unconsumed element).  Window [w, w + wlen) takes a prefix of what is
-      // left of each stream, w being the smaller of the two cursor values.
-      // One pass inserts from both streams' current chunks (one barrier); a
-      // stream is finished for the window once an element past it is seen.
-      if (!wait_chunk(barA, 0) || !wait_chunk(barB, 0)) aborted = true;
-      uint32_t qa0, qa1, qb0, qb1;
-      qrange(xa, 0, qa0, qa1);
-      qrange(xb, 0, qb0, qb1);
-      uint32_t curA = qa0, curB = qb0;
-      bool doneA = false, doneB = false;
-      uint32_t pass = 0;
-      if (t < 6) s_bound[t] = 0xffffffffu;
-      __syncthreads();
-      constexpr int NWP = NT / 32;        // warps
-      constexpr int WPW = BMW / NWP;      // table words per warp
-      constexpr int KW = WPW / 32;        // words per lane
-      static_assert(WPW % 32 == 0, "table words per warp must be a multiple of 32");
-      while (!aborted) {
-        const uint32_t va = slotA[(ca % NS) * C + curA];
-        const uint32_t vb = slotB[(cb % NS) * C + curB];
-        const uint32_t w = va < vb ? va : vb;
-        const uint32_t wlen =
-            (uint64_t(w) + WIN > 0x100000000ull) ? uint32_t(0x100000000ull - w) : WIN;
-        bool actA = true, actB = true;  // still inserting into this window
-        while (actA || actB) {
-          uint32_t stopA = 0xffffffffu, stopB = 0xffffffffu;
+      // ================= dense: groups =================
+      uint32_t i0 = qa0;  // first slot index of the next group in chunk ca
+      uint32_t g = 0;     // groups run so far
+      uint32_t wprev = 0, zprev = 0;  // last group's base value, T words used
+      uint32_t bres = 0;  // first unconsumed index of the retained B chunk
+      bool more = true;
+      for (;;) {
+        // ---- phase 1: last group's output and clearing, next insertion ----
+        if (g > 0) {
+          uint32_t *tp = tab + ((g - 1) & 1u) * TW;
+          if (MAT && warp == int((g - 1) % NW)) {
+            // this group's extractor.  Lane l owns summary words
+            // [l*SPL, l*SPL + SPL), i.e. the M words they flag, in value order.
+            constexpr int SPL = Cfg::kSumWords >= 32 ? Cfg::kSumWords / 32 : 1;
+            const bool own = lane * SPL < Cfg::kSumWords;
+            uint32_t sw[SPL];
+            uint32_t pc = 0;
 #pragma unroll
-          for (int sidx = 0; sidx < 2; ++sidx) {
-            const bool isA = sidx == 0;
-            if (!(isA ? actA : actB)) continue;
-            const Stream &x = isA ? xa : xb;
-            const uint32_t c = isA ? ca : cb;
-            const uint32_t cur = isA ? curA : curB;
-            const uint32_t *sl = (isA ? slotA : slotB) + (c % NS) * C;
-            const uint32_t *sls = BSR ? (isA ? slotSA : slotSB) + (c % NS) * C : nullptr;
-            uint32_t *tab = isA ? tabA : tabB;
-            uint32_t q0, q1;
-            qrange(x, c, q0, q1);
-            const uint32_t g0 = cur >> 2, g1 = (q1 + 3) >> 2;
-            uint32_t stop = 0xffffffffu;
-            for (uint32_t g = g0 + t; g < g1; g += NT) {
-              const uint4 v4 = reinterpret_cast<const uint4 *>(sl)[g];
-              const uint32_t qb = 4 * g;
-              const uint32_t o[4] = {v4.x - w, v4.y - w, v4.z - w, v4.w - w};
-              const bool edge = (g == g0) | (g + 1 == g1);
-              uint32_t outm = 0;
+            for (int k = 0; k < SPL; ++k) {
+              sw[k] = own ? msum[lane * SPL + k] : 0u;
+              uint32_t f = sw[k];
+              while (f) {
+                const uint32_t mi = uint32_t(lane * SPL + k) * 32u + uint32_t(__ffs(f) - 1);
+                f &= f - 1;
+                pc += __popc(mbits[mi]);
+              }
+            }
+            uint32_t incl = pc;
 #pragma unroll
-              for (int e2 = 0; e2 < 4; ++e2) {
-                const bool valid = !edge || ((qb + e2 >= cur) && (qb + e2 < q1));
-                const bool in = valid && (o[e2] < wlen);
-                if (in) {
-                  if (BSR) tab[o[e2]] = sls[qb + e2];
-                  else atomicOr(&tab[o[e2] >> 5], 1u << (o[e2] & 31u));
+            for (int of = 1; of < 32; of <<= 1) {
+              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, of);
+              if (lane >= of) incl += y;
+            }
+            const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+            const uint64_t base = s_cnt;  // matches staged by earlier groups
+            uint64_t q = base + incl - pc;
+#pragma unroll
+            for (int k = 0; k < SPL; ++k) {
+              uint32_t f = sw[k];
+              if (f) msum[lane * SPL + k] = 0;
+              while (f) {
+                const uint32_t mi = uint32_t(lane * SPL + k) * 32u + uint32_t(__ffs(f) - 1);
+                f &= f - 1;
+                uint32_t m = mbits[mi];
+                mbits[mi] = 0;
+                while (m) {
+                  const uint32_t off = mi * 32u + uint32_t(__ffs(m) - 1);  // value (base) offset
+                  m &= m - 1;
+                  if (q < cap) {
+                    p.stage[stage_base + q] = wprev + off;
+                    if (BSR) p.stage_s[stage_base + q] = tp[off];
+                  }
+                  ++q;
                 }
-                outm |= uint32_t(valid && !in) << e2;
-              }
-              if (outm) {
-                stop = qb + uint32_t(__ffs(outm) - 1);
-                break;
               }
             }
-            if (isA) stopA = stop;
-            else stopB = stop;
+            __syncwarp();
+            if (lane == 0) s_cnt = base + tot;
+            if (BSR) {
+              // the extractor read T's states: it also clears T
+              const uint32_t zr = (zprev + 3u) & ~3u;
+              for (uint32_t i = 4u * uint32_t(lane); i < zr; i += 128u)
+                *reinterpret_cast<uint4 *>(tp + i) = make_uint4(0, 0, 0, 0);
+            }
           }
-          const uint32_t wsa = __reduce_min_sync(0xffffffffu, stopA);
-          const uint32_t wsb = __reduce_min_sync(0xffffffffu, stopB);
-          const uint32_t slot = (pass % 3) * 2;
-          if (lane == 0) {
-            if (wsa != 0xffffffffu) atomicMin(&s_bound[slot], wsa);
-            if (wsb != 0xffffffffu) atomicMin(&s_bound[slot + 1], wsb);
+          if (!MAT || !BSR) {
+            // clear the last group's T words, warp by warp
+            constexpr uint32_t RW = uint32_t(VW / NW);
+            const uint32_t rb = uint32_t(warp) * RW;
+            const uint32_t zr = (zprev + 3u) & ~3u;
+            const uint32_t re = (rb + RW < zr) ? rb + RW : zr;
+            for (uint32_t i = rb + 4u * uint32_t(lane); i < re; i += 128u)
+              *reinterpret_cast<uint4 *>(tp + i) = make_uint4(0, 0, 0, 0);
           }
-          __syncthreads();  // chunk reads and bounds done
-          const uint32_t bA = s_bound[slot], bB = s_bound[slot + 1];
-          if (t < 2) s_bound[((pass + 2) % 3) * 2 + t] = 0xffffffffu;
-          ++pass;
-          bool waitA = false, waitB = false;
+        }
+        if (!more) break;
+
+        // ---- group g: A[i0, i1) of chunk ca ----
+        mbar_wait_abortable(&fullA[ca % NSA], (ca / NSA) & 1u, p.err, abortp);
+        const uint32_t *sa = slotA + (ca % NSA) * C;
+        const uint32_t *ssa = BSR ? slotSA + (ca % NSA) * C : nullptr;
+        const uint32_t w = sa[i0];
+        uint32_t i1 = qa1;
+        if (sa[qa1 - 1] - w >= SPAN) {
+          // first index past i0 whose value is >= w + SPAN
+          uint32_t lo = i0 + 1, len = qa1 - lo;
+          while (len > 0) {
+            const uint32_t h = len >> 1;
+            if (sa[lo + h] - w < SPAN) {
+              lo += h + 1;
+              len -= h + 1;
+            } else {
+              len = h;
+            }
+          }
+          i1 = lo;
+        }
+        const uint32_t alast = sa[i1 - 1];
+        const uint32_t span = (alast - w < SPAN) ? alast - w : SPAN - 1;
+        uint32_t *tg = tab + (g & 1u) * TW;
+        for (uint32_t u = (i0 >> 2) + uint32_t(t); u < ((i1 + 3) >> 2); u += NT) {
+          const uint4 v4 = reinterpret_cast<const uint4 *>(sa)[u];
+          const uint32_t o[4] = {v4.x - w, v4.y - w, v4.z - w, v4.w - w};
+          uint32_t okm = 0xfu;  // slots inside [i0, i1)
+          const uint32_t q = 4 * u;
+          if (q < i0 || q + 4 > i1) {
 #pragma unroll
-          for (int sidx = 0; sidx < 2; ++sidx) {
-            const bool isA = sidx == 0;
-            bool &act = isA ? actA : actB;
-            if (!act) continue;
-            const uint32_t bnd = isA ? bA : bB;
-            if (bnd != 0xffffffffu) {  // the window ends inside this chunk
-              (isA ? curA : curB) = bnd;
-              act = false;
-              continue;
-            }
-            const Stream &x = isA ? xa : xb;
-            uint32_t &c = isA ? ca : cb;
-            refill(x, isA ? slotA : slotB, isA ? slotSA : slotSB, isA ? barA : barB,
-                   c, isA ? issuedA : issuedB);
-            ++c;
-            if (c >= x.nc) {
-              (isA ? doneA : doneB) = true;
-              act = false;
-              continue;
-            }
-            uint32_t n0, n1;
-            qrange(x, c, n0, n1);
-            (isA ? curA : curB) = n0;
-            (isA ? waitA : waitB) = true;
+            for (int e = 0; e < 4; ++e)
+              if (q + e < i0 || q + e >= i1) okm &= ~(1u << e);
           }
-          if (waitA || waitB) {
-            bool ok = true;
-            if (waitA) ok = mbar_wait_bounded(&barA[ca % NS], (ca / NS) & 1u, p.err);
-            if (ok && waitB) ok = mbar_wait_bounded(&barB[cb % NS], (cb / NS) & 1u, p.err);
-            if (__syncthreads_or(!ok)) {
-              aborted = true;
+          if (BSR) {
+            const uint4 s4 = reinterpret_cast<const uint4 *>(ssa)[u];
+            const uint32_t st[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if ((okm >> e) & 1u) tg[o[e] & (SPAN - 1)] = st[e];
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if ((okm >> e) & 1u) atomicOr(&tg[(o[e] & (SPAN - 1)) >> 5], 1u << (o[e] & 31));
+          }
+        }
+        if (i1 == qa1) {  // chunk used up: release it
+          release_a(ca);
+          ++ca;
+          if (ca < xa.nc) {
+            qrange(xa, ca, qa0, qa1);
+            i0 = qa0;
+          }
+        } else {
+          i0 = i1;
+        }
+        const bool a_left = ca < xa.nc;
+        __syncthreads();  // T(g) complete; the last group's output written
+
+        // ---- phase 2: probe B chunks against T(g) ----
+        const uint32_t oclamp = span + 1;  // offset of a zero bit / word
+        bool bdone = false;
+        for (;;) {
+          mbar_wait_abortable(&fullB[cb % NSB], (cb / NSB) & 1u, p.err, abortp);
+          const uint32_t *sb = slotB + (cb % NSB) * C;
+          const uint32_t *ssb = BSR ? slotSB + (cb % NSB) * C : nullptr;
+          qrange(xb, cb, qb0, qb1);
+          const uint32_t qs = bres > qb0 ? bres : qb0;  // skip what is consumed
+          const uint32_t bmax = sb[qb1 - 1];
+          const bool keep = bmax > alast;  // chunk outlives this group
+          uint32_t qe = qb1;
+          if (keep) {
+            // first index whose value is past the group (exists: bmax > alast)
+            uint32_t lo = qs, len = qb1 - qs;
+            while (len > 0) {
+              const uint32_t h = len >> 1;
+              if (sb[lo + h] <= alast) {
+                lo += h + 1;
+                len -= h + 1;
+              } else {
+                len = h;
+              }
+            }
+            qe = lo;
+          }
+          for (uint32_t u = (qs >> 2) + uint32_t(t); u < ((qe + 3) >> 2); u += NT) {
+            const uint4 v4 = reinterpret_cast<const uint4 *>(sb)[u];
+            uint32_t o[4] = {v4.x - w, v4.y - w, v4.z - w, v4.w - w};
+            const uint32_t q = 4 * u;
+            if (q < qs || q + 4 > qe) {
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                if (q + e < qs || q + e >= qe) o[e] = oclamp;
+            }
+            uint32_t hit = 0, wd[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              o[e] = o[e] < oclamp ? o[e] : oclamp;
+              wd[e] = tg[BSR ? o[e] : (o[e] >> 5)];
+            }
+            uint32_t st[4] = {0, 0, 0, 0};
+            if (BSR) {
+              const uint4 s4 = reinterpret_cast<const uint4 *>(ssb)[u];
+              st[0] = s4.x; st[1] = s4.y; st[2] = s4.z; st[3] = s4.w;
+#pragma unroll
+              for (int e = 0; e < 4; ++e) hit |= uint32_t((wd[e] & st[e]) != 0) << e;
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) hit |= ((wd[e] >> (o[e] & 31)) & 1u) << e;
+            }
+            if (hit) {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                if (!((hit >> e) & 1u)) continue;
+                if (MAT) {
+                  if (BSR) tg[o[e]] = wd[e] & st[e];
+                  const uint32_t mw = o[e] >> 5;
+                  if (atomicOr(&mbits[mw], 1u << (o[e] & 31)) == 0u)
+                    atomicOr(&msum[mw >> 5], 1u << (mw & 31));  // first bit of the word
+                } else {
+                  cnt += BSR ? __popc(wd[e] & st[e]) : 1u;
+                }
+              }
+            }
+          }
+          if (!keep) {  // chunk used up: release it
+            release_b(cb);
+            bres = 0;
+            ++cb;
+            if (cb >= xb.nc) {
+              bdone = true;
               break;
             }
-          }
-        }
-        if (aborted) break;
-        // AND the two tables.  Warp wp owns words [wp*WPW, (wp+1)*WPW), lane l
-        // words wp*WPW + 32k + l (conflict-free); word order = value order.
-        const int wp = t >> 5;
-        uint32_t *ta = tabA + wp * WPW + lane;
-        uint32_t *tb = tabB + wp * WPW + lane;
-        uint32_t hits = 0;
-#pragma unroll 4
-        for (int k = 0; k < KW; ++k) {
-          const uint32_t m = ta[32 * k] & tb[32 * k];
-          tb[32 * k] = 0;
-          ta[32 * k] = MAT ? m : 0u;
-          if (BSR) {
-            if (MAT) hits += (m != 0);
-            else cnt += __popc(m);
           } else {
-            hits += __popc(m);
+            bres = qe;
           }
+          if (bmax >= alast) break;  // group used up
         }
-        if (MAT) {
-          // warp totals -> block offsets (only when the window has matches)
-          uint32_t wt = hits;
-#pragma unroll
-          for (int of = 16; of > 0; of >>= 1) wt += __shfl_xor_sync(0xffffffffu, wt, of);
-          if (__syncthreads_or(hits != 0)) {
-            if (lane == 0) warp_sums[wp] = wt;
-            __syncthreads();
-            uint32_t woff = 0, tot = 0;
-#pragma unroll
-            for (int i = 0; i < NWP; ++i) {
-              const uint32_t v = warp_sums[i];
-              woff += (i < wp) ? v : 0u;
-              tot += v;
-            }
-            uint64_t o = stage_base + cta_cnt + woff;
-            for (int k = 0; k < KW; ++k) {
-              uint32_t m = ta[32 * k];
-              if (!__any_sync(0xffffffffu, m != 0)) continue;
-              ta[32 * k] = 0;
-              const uint32_t pc = BSR ? uint32_t(m != 0) : uint32_t(__popc(m));
-              uint32_t incl = pc;
-#pragma unroll
-              for (int of = 1; of < 32; of <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, of);
-                if (lane >= of) incl += y;
-              }
-              uint64_t q = o + incl - pc;
-              const uint32_t wbase = w + uint32_t(wp * WPW + 32 * k + lane) * (BSR ? 1u : 32u);
-              if (BSR) {
-                if (m) {
-                  p.stage[q] = wbase;
-                  p.stage_s[q] = m;
-                }
-              } else {
-                while (m) {
-                  p.stage[q++] = wbase + uint32_t(__ffs(m) - 1);
-                  m &= m - 1;
-                }
-              }
-              o += __shfl_sync(0xffffffffu, incl, 31);
-            }
-            cta_cnt += tot;
-          }
-          // every nonzero AND word was extracted and cleared above
-        } else if (!BSR) {
-          cnt += hits;
-        }
-        __syncthreads();  // tables clear before the next window's inserts
-        // one run used up: nothing left in the other can match
-        if (doneA || doneB) break;
-        if (uint64_t(w) + wlen >= 0x100000000ull) break;
+        wprev = w;
+        zprev = BSR ? span + 1 : (span >> 5) + 1;
+        ++g;
+        // one run used up (nothing left in the other can match), or a wait
+        // gave up: the next phase 1 is the last
+        more = !__syncthreads_or(bdone || !a_left || *abortp != 0u);
+      }
+      if (MAT) {
+        __syncthreads();  // the last extraction's count reaches every warp
+        cta_cnt = s_cnt;
       }
     } else {
       // ============ sparse: chunk pairs, binary search of A in B ============
-      if (!wait_chunk(barA, 0) || !wait_chunk(barB, 0)) aborted = true;
-      while (!aborted) {
-        const uint32_t *sa = slotA + (ca % NS) * C;
-        const uint32_t *ssa = BSR ? slotSA + (ca % NS) * C : nullptr;
-        const uint32_t *sb = slotB + (cb % NS) * C;
-        const uint32_t *ssb = BSR ? slotSB + (cb % NS) * C : nullptr;
-        uint32_t qa0, qa1, qb0, qb1;
+      constexpr uint32_t PER = (C + NT - 1) / NT;
+      for (;;) {
+        mbar_wait_abortable(&fullA[ca % NSA], (ca / NSA) & 1u, p.err, abortp);
+        mbar_wait_abortable(&fullB[cb % NSB], (cb / NSB) & 1u, p.err, abortp);
+        const uint32_t *sa = slotA + (ca % NSA) * C;
+        const uint32_t *ssa = BSR ? slotSA + (ca % NSA) * C : nullptr;
+        const uint32_t *sb = slotB + (cb % NSB) * C;
+        const uint32_t *ssb = BSR ? slotSB + (cb % NSB) * C : nullptr;
         qrange(xa, ca, qa0, qa1);
         qrange(xb, cb, qb0, qb1);
         const uint32_t bmin = sb[qb0], bmax = sb[qb1 - 1];
         const uint32_t amax = sa[qa1 - 1];
-        // thread t: contiguous A elements [qa0 + t*per, ...) in order
-        constexpr uint32_t PER = (C + NT - 1) / NT;
+        // thread t: contiguous A elements [qa0 + t*PER, ...) in order
         const uint32_t my0 = qa0 + uint32_t(t) * PER;
         uint32_t hits = 0;
         auto find = [&](uint32_t v, uint32_t &st) -> bool {
@@ -630,25 +785,21 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
         }
         if (MAT) {
           uint32_t tot;
-          const uint32_t ex = block_exclusive_scan<NT>(hits, warp_sums, &tot);
+          const uint32_t ex = scan_exclusive_nb<NT>(hits, warp_sums, &tot);
           if (hits) {
-            uint32_t *dst = p.stage + stage_base + cta_cnt + ex;
-            uint32_t *dsts = BSR ? p.stage_s + stage_base + cta_cnt + ex : nullptr;
-            uint32_t o = 0;
+            uint64_t o = cta_cnt + ex;
             for (uint32_t i = 0; i < PER; ++i) {
               const uint32_t q = my0 + i;
               if (q >= qa1) break;
               uint32_t st = 0;
               if (find(sa[q], st)) {
-                if (BSR) {
-                  st &= ssa[q];
-                  if (st) {
-                    dst[o] = sa[q];
-                    dsts[o] = st;
-                    ++o;
+                if (BSR) st &= ssa[q];
+                if (!BSR || st) {
+                  if (o < cap) {
+                    p.stage[stage_base + o] = sa[q];
+                    if (BSR) p.stage_s[stage_base + o] = st;
                   }
-                } else {
-                  dst[o++] = sa[q];
+                  ++o;
                 }
               }
             }
@@ -657,33 +808,35 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
         } else if (!BSR) {
           cnt += hits;
         }
-        __syncthreads();  // chunk reads done
         const bool advA = amax <= bmax, advB = bmax <= amax;
         if (advA) {
-          refill(xa, slotA, slotSA, barA, ca, issuedA);
+          release_a(ca);
           ++ca;
         }
         if (advB) {
-          refill(xb, slotB, slotSB, barB, cb, issuedB);
+          release_b(cb);
           ++cb;
         }
-        if (ca >= xa.nc || cb >= xb.nc) break;
-        if (advA && !wait_chunk(barA, ca)) { aborted = true; break; }
-        if (advB && !wait_chunk(barB, cb)) { aborted = true; break; }
+        const bool stop = ca >= xa.nc || cb >= xb.nc;
+        if (MAT) {
+          // the scan above holds barriers: leave together
+          if (__syncthreads_or(stop || *abortp != 0u)) break;
+        } else if (stop) {
+          break;
+        }
       }
     }
   }
 
-  // ---- drain: every issued chunk must have landed before exit ----
+  // every thread is past its last wait and issue: no copy may still be in
+  // flight when the CTA exits
+  const bool aborted = __syncthreads_or(*abortp != 0u);
   if (t == 0) {
-    // chunks [first unwaited, issued) may still be in flight
-    const uint32_t fa = ca, fb = cb;
-    for (uint32_t c = fa; c < issuedA; ++c)
-      mbar_wait_bounded(&barA[c % NS], (c / NS) & 1u, p.err);
-    for (uint32_t c = fb; c < issuedB; ++c)
-      mbar_wait_bounded(&barB[c % NS], (c / NS) & 1u, p.err);
+    for (int s = 0; s < NSA; ++s)
+      if (lastA[s]) mbar_wait_bounded(&fullA[s], ((lastA[s] - 1) / NSA) & 1u, p.err);
+    for (int s = 0; s < NSB; ++s)
+      if (lastB[s]) mbar_wait_bounded(&fullB[s], ((lastB[s] - 1) / NSB) & 1u, p.err);
   }
-  __syncthreads();
   if (aborted) return;
 
   // ---- 3. combine ----
@@ -691,11 +844,11 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
     uint64_t v = cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[t >> 5] = v;
+    if (lane == 0) red[warp] = v;
     __syncthreads();
     if (t == 0) {
       unsigned long long s = 0;
-      for (int w = 0; w < NT / 32; ++w) s += red[w];
+      for (int w = 0; w < NW; ++w) s += red[w];
       if (s) atomicAdd(&p.sync->acc, s);
       __threadfence();
       const uint32_t prev = atomicAdd(&p.sync->done, 1u);
@@ -710,19 +863,13 @@ __global__ void __launch_bounds__(NT, (merge_min_blocks<NT, C, NS, BMW, BSR, MAT
     return;
   }
 
-  // materialise: decoupled look-back over CTA ranges (warp 0)
-  if (t < 32) {
-    const uint64_t ex =
-        lookback_exclusive_warp(p.status, vid, cta_cnt, p.epoch, p.err);
-    if (t == 0) {
-      s_excl = ex;
-      if (ex != UINT64_MAX && ex + cta_cnt > p.out_cap)
-        record_error(p.err, DEV_ERR_CAPACITY);
-    }
+  // materialise: output offset = sum of the predecessors' match counts
+  const uint64_t ex = predecessor_sum<NT>(p.status, vid, cta_cnt, p.epoch, p.err, red);
+  if (ex == UINT64_MAX) return;
+  if (ex + cta_cnt > p.out_cap || cta_cnt > cap) {
+    if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
+    return;
   }
-  __syncthreads();
-  const uint64_t ex = s_excl;
-  if (ex == UINT64_MAX || ex + cta_cnt > p.out_cap) return;
   for (uint64_t q = t; q < cta_cnt; q += NT) {
     p.out[ex + q] = p.stage[stage_base + q];
     if (BSR) p.out_s[ex + q] = p.stage_s[stage_base + q];
