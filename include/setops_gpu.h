@@ -161,6 +161,35 @@ int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
                          const size_t *lens, size_t k, uint64_t *count,
                          unsigned flags);
 
+/* ---- 2-set without allocation ----------------------------------------------
+ * No counterpart in the reference: it exists for callers of this library that
+ * cannot allocate device memory -- a host program that owns all device
+ * memory through its own pool, a latency-bound path that cannot take the
+ * device-wide synchronisation and unbounded latency of cudaMalloc/cudaFree,
+ * or a process whose GPU memory is already full.  The context API allocates
+ * (at setops_gpu_create, and scratch that grows with the input); this call
+ * allocates nothing and needs no context.
+ *
+ * Same result as setops_gpu_intersect on device pointers: a[0..na) and
+ * b[0..nb) are device arrays, out (device) receives the ascending
+ * intersection, out_cap >= min(na, nb), and *out_len (host) its length.  The
+ * work runs on `stream` (a cudaStream_t; NULL = the default stream) on the
+ * current device, and the call returns when it has finished.
+ *
+ * Its scratch is one fixed array that every GPU loading the library holds
+ * until the process exits, which limits the smaller input to
+ * SETOPS_NOALLOC_MAX_SMALL elements; larger calls return
+ * SETOPS_ERR_TOO_LARGE.  All calls on a device share that array: calls that
+ * overlapped on the GPU would race, so the call holds a per-device lock and
+ * returns only when its work is done.  The first call on a device sets up
+ * the array's device address (and the kernel's attributes); make that first
+ * call before any stream capture. */
+#define SETOPS_NOALLOC_MAX_SMALL ((size_t)1 << 20)
+int setops_gpu_intersect_noalloc(const uint32_t *a, size_t na,
+                                 const uint32_t *b, size_t nb, uint32_t *out,
+                                 size_t out_cap, size_t *out_len,
+                                 void *stream);
+
 /* ---- validation ----------------------------------------------------------
  * *is_sorted = 1 when a[0..n) is strictly increasing (no counterpart: the
  * reference debug_asserts this, setops/src/bsr.rs:71-72). */

@@ -76,6 +76,7 @@ SIGNATURES = [
     ("setops_gpu_svs", C.c_int, [vp, C.POINTER(vp), szp, sz, vp, sz, szp, uint]),
     ("setops_gpu_svs_count", C.c_int, [vp, C.POINTER(vp), szp, sz, u64p, uint]),
     ("setops_gpu_validate_sorted", C.c_int, [vp, vp, sz, C.POINTER(C.c_int), uint]),
+    ("setops_gpu_intersect_noalloc", C.c_int, [vp, sz, vp, sz, vp, sz, szp, vp]),
     # setops_bench.h
     ("setops_gen_twoset", C.c_int, [u64, C.c_double, C.c_double, sz, sz, vp, vp]),
     ("setops_gen_kset_lens", C.c_int, [sz, C.c_double, sz, szp]),
