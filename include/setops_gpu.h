@@ -59,6 +59,7 @@ enum {
 #define SETOPS_ALGO_AUTO (0u << SETOPS_ALGO_SHIFT)
 #define SETOPS_ALGO_MERGE (1u << SETOPS_ALGO_SHIFT)  /* merge-path kernel    */
 #define SETOPS_ALGO_GALLOP (2u << SETOPS_ALGO_SHIFT) /* search kernel        */
+#define SETOPS_ALGO_BITMAP (3u << SETOPS_ALGO_SHIFT) /* tiled bitmap kernel  */
 /* Variant of the chosen kernel (tile shape / probe group); 0 = default.
  * setops_gpu_num_variants() gives the count per algorithm. */
 #define SETOPS_VARIANT_SHIFT 16
@@ -81,14 +82,16 @@ void *setops_gpu_get_stream(setops_ctx *ctx);
 int setops_gpu_synchronize(setops_ctx *ctx);
 const char *setops_gpu_last_error(const setops_ctx *ctx);
 const char *setops_status_string(int status);
-/* Number of kernel variants of an algorithm (SETOPS_ALGO_MERGE / _GALLOP)
- * for the given element kind (0 = u32 arrays, 1 = BSR). */
+/* Number of kernel variants of an algorithm (SETOPS_ALGO_MERGE / _GALLOP /
+ * _BITMAP) for the given element kind (0 = u32 arrays, 1 = BSR; the bitmap
+ * kernel has no BSR variant, and a BSR call asking for it gets the merge). */
 int setops_gpu_num_variants(unsigned algo, int bsr);
 /* Number of kernels this context has launched (for launch accounting). */
 uint64_t setops_gpu_launch_count(const setops_ctx *ctx);
 /* Algorithm policy: the kernel used for pairs whose size ratio max/min lies
- * in [2^band, 2^(band+1)), band in [0, 32); algo_flags = SETOPS_ALGO_MERGE or
- * SETOPS_ALGO_GALLOP | SETOPS_VARIANT(v).  The autotuner writes this table;
+ * in [2^band, 2^(band+1)), band in [0, 32); algo_flags = SETOPS_ALGO_MERGE,
+ * SETOPS_ALGO_GALLOP or SETOPS_ALGO_BITMAP (arrays only) | SETOPS_VARIANT(v).
+ * The autotuner writes this table;
  * it plays the role of the reference's compile-time choice of algorithm per
  * ISA (setops/src/intersect.rs:26-36) and the benchmark's name registry
  * (benchmark/src/timer.rs:75-169). */

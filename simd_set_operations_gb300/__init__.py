@@ -30,7 +30,7 @@ from typing import Callable, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import (ALGO_AUTO, ALGO_GALLOP, ALGO_MERGE, HOST, VARIANT,
+from ._lib import (ALGO_AUTO, ALGO_BITMAP, ALGO_GALLOP, ALGO_MERGE, HOST, VARIANT,
                    SetopsError, lib)
 
 __all__ = [
@@ -41,7 +41,7 @@ __all__ = [
     "gpu_svs", "intersect", "intersect_count",
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
-    "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "VARIANT", "num_variants",
+    "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
 ]
 
 

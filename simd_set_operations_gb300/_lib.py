@@ -26,6 +26,7 @@ ALGO_SHIFT = 8
 ALGO_AUTO = 0 << ALGO_SHIFT
 ALGO_MERGE = 1 << ALGO_SHIFT
 ALGO_GALLOP = 2 << ALGO_SHIFT
+ALGO_BITMAP = 3 << ALGO_SHIFT
 VARIANT_SHIFT = 16
 
 

@@ -157,6 +157,12 @@ __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t *p) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void st_release_u64(uint64_t *p, uint64_t v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v)
                : "memory");

@@ -4,6 +4,7 @@
 
 #include "gallop.cuh"
 #include "merge.cuh"
+#include "tile.cuh"
 
 namespace setops {
 
@@ -22,6 +23,13 @@ KernelInfo mk_gallop(const char *name) {
   return KernelInfo{reinterpret_cast<const void *>(
                         &gallop_kernel<NT, GS, ITEMS, NSAMP, BSR, MAT>),
                     NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name};
+}
+
+template <int NT, int TA, int VW, bool MAT>
+KernelInfo mk_tile(const char *name) {
+  using Cfg = TileCfg<NT, TA, VW, MAT>;
+  return KernelInfo{reinterpret_cast<const void *>(&tile_kernel<NT, TA, VW, MAT>), NT,
+                    Cfg::kSmemBytes, TA, name, MAT};
 }
 
 // [variant][count, materialise]
@@ -49,6 +57,17 @@ const KernelInfo kMergeBsr[][2] = {
     MERGE_ROW(8, 2048, 2, 2, 4096, true),  // 1: 96 KB
     MERGE_ROW(8, 1024, 2, 2, 4096, true),  // 2: 64 KB
 };
+// NT threads; A tiles of TA elements; T of VW words (dense tiles span
+// < 32*VW values)
+#define TILE_ROW(NT, TA, VW)                                                   \
+  {mk_tile<NT, TA, VW, false>("bitmap_" #NT "_a" #TA "_t" #VW),                \
+   mk_tile<NT, TA, VW, true>("bitmap_" #NT "_a" #TA "_t" #VW)}
+const KernelInfo kBitmapU32[][2] = {
+    TILE_ROW(256, 4096, 4096),  // 0: 16 / 32 KB, 6 CTAs/SM
+    TILE_ROW(256, 2048, 2048),  // 1: smaller tiles, shorter tail
+    TILE_ROW(512, 4096, 4096),  // 2: 16 warps
+};
+
 // GS lanes per element (1 = thread per element with IT interleaved
 // searches); NS = shared-memory sample of the CTA's bracket (0 = none)
 const KernelInfo kGallopU32[][2] = {
@@ -75,6 +94,7 @@ constexpr int count_of(const T (&)[N]) {
 
 int num_variants(Algo algo, bool bsr) {
   if (algo == ALGO_MERGE) return bsr ? count_of(kMergeBsr) : count_of(kMergeU32);
+  if (algo == ALGO_BITMAP) return bsr ? 0 : count_of(kBitmapU32);
   return bsr ? count_of(kGallopBsr) : count_of(kGallopU32);
 }
 
@@ -83,6 +103,7 @@ const KernelInfo &variant(Algo algo, bool bsr, bool mat, int v) {
   if (v < 0 || v >= n) v = 0;
   const int m = mat ? 1 : 0;
   if (algo == ALGO_MERGE) return bsr ? kMergeBsr[v][m] : kMergeU32[v][m];
+  if (algo == ALGO_BITMAP && !bsr) return kBitmapU32[v][m];
   return bsr ? kGallopBsr[v][m] : kGallopU32[v][m];
 }
 

@@ -12,18 +12,20 @@ namespace setops {
 struct MergeArgs;
 struct GallopArgs;
 
-// One compiled kernel: entry point, block size, dynamic shared memory, and
-// the number of merged elements (merge) or small-set elements (search) one
-// tile covers.
+// One compiled kernel: entry point, block size, dynamic shared memory, the
+// number of merged elements (merge), small-set elements (search) or A
+// elements (bitmap) one tile covers, and whether it must be launched
+// cooperatively (all CTAs resident: it holds grid-wide barriers).
 struct KernelInfo {
   const void *fn;
   int nt;
   size_t dyn_smem;
   int tile;
   const char *name;
+  bool coop = false;
 };
 
-enum Algo { ALGO_MERGE = 1, ALGO_GALLOP = 2 };
+enum Algo { ALGO_MERGE = 1, ALGO_GALLOP = 2, ALGO_BITMAP = 3 };
 
 int num_variants(Algo algo, bool bsr);
 // kind: 0 count, 1 materialise

@@ -183,6 +183,12 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
     c.variant = var;
     return c;
   }
+  if (algo == SETOPS_ALGO_BITMAP) {
+    // arrays only; BSR sets take the merge kernel
+    c.algo = bsr ? ALGO_MERGE : ALGO_BITMAP;
+    c.variant = bsr ? 0 : var;
+    return c;
+  }
   const uint64_t mn = std::min(na, nb), mx = std::max(na, nb);
   if (mn == 0) {
     c.algo = ALGO_GALLOP;
@@ -192,8 +198,10 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
   int band = 0;
   for (uint64_t r = mx / mn; r > 1 && band < kRatioBands - 1; r >>= 1) ++band;
   const unsigned pol = ctx->policy[bsr ? 1 : 0][band];
-  c.algo = ((pol & SETOPS_ALGO_MASK) == SETOPS_ALGO_GALLOP) ? ALGO_GALLOP
-                                                             : ALGO_MERGE;
+  const unsigned pa = pol & SETOPS_ALGO_MASK;
+  c.algo = (pa == SETOPS_ALGO_GALLOP)               ? ALGO_GALLOP
+           : (pa == SETOPS_ALGO_BITMAP && !bsr)     ? ALGO_BITMAP
+                                                    : ALGO_MERGE;
   c.variant = int((pol & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
   return c;
 }
@@ -210,13 +218,14 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // ratio < 32: merge-path; 32..511: sampled thread-per-element search;
-    // 512..8191: 16 lanes per element; >= 8192: a warp per element.
+    // arrays: ratio < 4: tiled bitmap; 4..31: merge-path; 32..511: sampled
+    // thread-per-element search; 512..8191: 16 lanes per element; >= 8192: a
+    // warp per element.  BSR: merge-path below 32.
     unsigned v = (b < 5)    ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
                  : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
                  : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(1))
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
-    unsigned u = v, s = v;
+    unsigned u = (b < 2) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(0)) : v, s = v;
     ctx->policy[0][b] = u;
     ctx->policy[1][b] = s;
   }
@@ -234,11 +243,18 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   RK(ctx_occupancy(ctx, k, &occ));
   const uint64_t full = uint64_t(occ) * uint64_t(ctx->sms);
   uint64_t grid = 1, status_words = 1;
+  uint64_t ntiles = 0;
   if (j.choice.algo == ALGO_MERGE) {
     const uint64_t total = na_ub + nb_ub;
     const uint64_t per = uint64_t(k.tile) * kMinTilesPerCta;
     grid = std::max<uint64_t>(1, std::min(full, (total + per - 1) / per));
     status_words = grid;
+  } else if (j.choice.algo == ALGO_BITMAP) {
+    // persistent grid over tiles of the smaller set; per-tile counts, then
+    // per-CTA block totals
+    ntiles = (mn + k.tile - 1) / k.tile;
+    grid = std::max<uint64_t>(1, std::min(full, ntiles));
+    status_words = std::max<uint64_t>(ntiles, 1);
   } else {
     const uint64_t ntiles = (mn + k.tile - 1) / k.tile;
     grid = std::max<uint64_t>(1, std::min(full, ntiles));
@@ -247,7 +263,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   if (j.grid_cap && grid > j.grid_cap) grid = j.grid_cap;
   uint32_t epoch = 0;
   // merge kernels publish per-CTA co-ranks after the look-back words
-  const bool merge = j.choice.algo == ALGO_MERGE;
+  const bool merge = j.choice.algo == ALGO_MERGE || j.choice.algo == ALGO_BITMAP;
   RK(ctx_status_words(ctx, merge ? status_words + grid : status_words));
   RK(ctx_next_epoch(ctx, &epoch));
   LaunchSync *sync = ctx->sync + j.sync_slot;
@@ -261,7 +277,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
       stage_s = static_cast<uint32_t *>(ctx->stage1.p);
     }
   }
-  if (j.choice.algo == ALGO_MERGE) {
+  if (j.choice.algo == ALGO_MERGE || j.choice.algo == ALGO_BITMAP) {
     MergeArgs a{};
     a.a = j.a;
     a.b = j.b;
@@ -278,7 +294,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     a.out_cap = j.out_cap;
     a.out_len = j.len_dev;
     a.status = static_cast<uint64_t *>(ctx->status.p);
-    a.coranks = static_cast<uint64_t *>(ctx->status.p) + grid;
+    a.coranks = static_cast<uint64_t *>(ctx->status.p) + status_words;
     a.sync = sync;
     a.err = ctx->derr;
     a.epoch = epoch;
@@ -318,8 +334,11 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
 // Launches kernel k with one argument block; errors name the launch shape.
 int ctx_launch(setops_ctx *ctx, const KernelInfo &k, uint64_t grid,
                void **args) {
-  const cudaError_t e = cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt),
-                                         args, k.dyn_smem, ctx->st);
+  const cudaError_t e =
+      k.coop ? cudaLaunchCooperativeKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args,
+                                           k.dyn_smem, ctx->st)
+             : cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args, k.dyn_smem,
+                                ctx->st);
   if (e == cudaSuccess) return SETOPS_OK;
   char buf[256];
   std::snprintf(buf, sizeof buf, "launch of %s (grid %llu, block %d, %zu B shared)",
@@ -431,6 +450,8 @@ int setops_gpu_num_variants(unsigned algo, int bsr) {
     return num_variants(ALGO_MERGE, bsr != 0);
   if ((algo & SETOPS_ALGO_MASK) == SETOPS_ALGO_GALLOP)
     return num_variants(ALGO_GALLOP, bsr != 0);
+  if ((algo & SETOPS_ALGO_MASK) == SETOPS_ALGO_BITMAP)
+    return num_variants(ALGO_BITMAP, bsr != 0);
   return 0;
 }
 
@@ -442,10 +463,11 @@ int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
                           unsigned algo_flags) {
   if (!ctx || ratio_band < 0 || ratio_band >= kRatioBands) return SETOPS_ERR_INVALID;
   const unsigned a = algo_flags & SETOPS_ALGO_MASK;
-  if (a != SETOPS_ALGO_MERGE && a != SETOPS_ALGO_GALLOP) return SETOPS_ERR_INVALID;
-  const int v = int((algo_flags & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
-  if (v >= num_variants(a == SETOPS_ALGO_MERGE ? ALGO_MERGE : ALGO_GALLOP, bsr != 0))
+  if (a != SETOPS_ALGO_MERGE && a != SETOPS_ALGO_GALLOP && a != SETOPS_ALGO_BITMAP)
     return SETOPS_ERR_INVALID;
+  const int v = int((algo_flags & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+  const Algo al = a == SETOPS_ALGO_MERGE ? ALGO_MERGE : a == SETOPS_ALGO_GALLOP ? ALGO_GALLOP : ALGO_BITMAP;
+  if (v >= num_variants(al, bsr != 0)) return SETOPS_ERR_INVALID;
   ctx->policy[bsr ? 1 : 0][ratio_band] =
       algo_flags & (SETOPS_ALGO_MASK | SETOPS_VARIANT_MASK);
   return SETOPS_OK;

@@ -20,6 +20,7 @@ def all_algos():
     algos = [so.ALGO_AUTO]
     algos += [so.ALGO_MERGE | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_MERGE))]
     algos += [so.ALGO_GALLOP | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_GALLOP))]
+    algos += [so.ALGO_BITMAP | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_BITMAP))]
     return algos
 
 
@@ -116,7 +117,8 @@ def test_device_pointers_and_misalignment(ctx, orc):
             ta[off_a:off_a + a.size] = torch.from_numpy(a.view(np.int32))
             tb[off_b:off_b + b.size] = torch.from_numpy(b.view(np.int32))
             va, vb = ta[off_a:off_a + a.size], tb[off_b:off_b + b.size]
-            for algo in (so.ALGO_MERGE, so.ALGO_GALLOP, so.ALGO_MERGE | so.VARIANT(2)):
+            for algo in (so.ALGO_MERGE, so.ALGO_GALLOP, so.ALGO_MERGE | so.VARIANT(2),
+                         so.ALGO_BITMAP, so.ALGO_BITMAP | so.VARIANT(1)):
                 out, n = so.intersect(va, vb, algo=algo, ctx=ctx)
                 got = out[:n].cpu().numpy().view(np.uint32)
                 assert np.array_equal(got, want), (off_a, off_b, hex(algo))
