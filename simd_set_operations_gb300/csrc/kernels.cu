@@ -25,10 +25,10 @@ KernelInfo mk_gallop(const char *name) {
                     NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name};
 }
 
-template <int NT, int TA, int VW, bool MAT>
+template <int NT, int TA, int VW, int MINB, bool MAT>
 KernelInfo mk_tile(const char *name) {
   using Cfg = TileCfg<NT, TA, VW, MAT>;
-  return KernelInfo{reinterpret_cast<const void *>(&tile_kernel<NT, TA, VW, MAT>), NT,
+  return KernelInfo{reinterpret_cast<const void *>(&tile_kernel<NT, TA, VW, MINB, MAT>), NT,
                     Cfg::kSmemBytes, TA, name, MAT};
 }
 
@@ -58,14 +58,15 @@ const KernelInfo kMergeBsr[][2] = {
     MERGE_ROW(8, 1024, 2, 2, 4096, true),  // 2: 64 KB
 };
 // NT threads; A tiles of TA elements; T of VW words (dense tiles span
-// < 32*VW values)
-#define TILE_ROW(NT, TA, VW)                                                   \
-  {mk_tile<NT, TA, VW, false>("bitmap_" #NT "_a" #TA "_t" #VW),                \
-   mk_tile<NT, TA, VW, true>("bitmap_" #NT "_a" #TA "_t" #VW)}
+// < 32*VW values); MINB CTAs per SM the register budget allows
+#define TILE_ROW(NT, TA, VW, MINB)                                             \
+  {mk_tile<NT, TA, VW, MINB, false>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB), \
+   mk_tile<NT, TA, VW, MINB, true>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB)}
 const KernelInfo kBitmapU32[][2] = {
-    TILE_ROW(256, 4096, 4096),  // 0: 16 / 32 KB, 6 CTAs/SM
-    TILE_ROW(256, 2048, 2048),  // 1: smaller tiles, shorter tail
-    TILE_ROW(512, 4096, 4096),  // 2: 16 warps
+    TILE_ROW(256, 4096, 4096, 8),  // 0: 16 / 32 KB shared; 8 CTAs/SM (count), 7 (mat.)
+    TILE_ROW(256, 4096, 4096, 6),  // 1: 6 CTAs/SM
+    TILE_ROW(256, 2048, 2048, 8),  // 2: smaller tiles
+    TILE_ROW(256, 4096, 4096, 4),  // 3: more registers per thread
 };
 
 // GS lanes per element (1 = thread per element with IT interleaved

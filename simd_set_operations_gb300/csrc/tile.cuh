@@ -5,31 +5,32 @@
 //
 // Work layout
 // -----------
-// Let A be the smaller input.  A is cut into fixed tiles of TA elements;
-// a persistent grid pulls tiles in order from an atomic ticket.  For tile t
-// covering A[i0, i1) with values [w, alast]:
+// Let A be the smaller input.  CTA c of the G resident CTAs owns the
+// contiguous run A[c*na/G, (c+1)*na/G) and walks it in tiles of up to TA
+// elements.  For a tile A[i0, i1) with values [w, alast]:
 //
-//   1. Two warps find the tile's B range [b0, b1) -- the B elements with
-//      values in [w, alast] -- by warp-wide searches of B in global memory,
-//      while the other warps stream A[i0, i1) with 128-bit loads: into a
-//      bitmap T of the value range when it is dense enough (span < 32*VW),
-//      else as the sorted A tile itself.
+//   1. Warp 0 finds where the tile's B range ends, b1 = the first B index
+//      with a value above alast, by a warp-wide search of B in global memory
+//      (the range starts where the previous tile's ended; the CTA's first
+//      tile searches its start too, on warp 1), while the other warps stream
+//      A[i0, i1) with 128-bit loads: into a bitmap T of the value range when
+//      it is dense enough (span < 32*VW), else as the sorted A tile itself.
 //   2. All warps stream B[b0, b1) with 128-bit loads; each element tests its
 //      bit in T (dense) or binary-searches the A tile (sparse).
 //   3. Count mode counts.  Materialise mode marks each match in bitmap M
 //      (by value offset when dense, by A position when sparse; either way M
-//      is in ascending order) and writes the tile's matches, in order, to a
-//      staging area at i0 -- an exclusive region, since a tile cannot match
-//      more elements than it has.
+//      is in ascending order) and appends the tile's matches, in order, to
+//      the CTA's staging run, which starts at the CTA's first A index -- an
+//      exclusive region, since a CTA cannot match more elements than it owns.
 //
-// Materialise mode ends with one grid-wide barrier (the kernel is launched
-// cooperatively, so every CTA is resident), after which every CTA scans the
-// per-tile match counts and copies its share of the tiles' staged matches to
-// their final offsets.  Count mode adds per-CTA totals atomically.
+// Materialise mode then publishes each CTA's match count, passes one
+// grid-wide barrier (the kernel is launched cooperatively, so every CTA is
+// resident) and copies the CTA's staged run to its offset, the sum of the
+// counts of CTAs 0..c-1.  Count mode adds per-CTA totals atomically.
 //
 // There are no mbarriers and no asynchronous copies: every input element is
-// read once with a coalesced 128-bit load (boundary elements with plain
-// loads), and the only waits are the bounded grid barrier and nothing else.
+// read once with a coalesced 128-bit load (ragged ends with plain loads);
+// the only wait is the bounded grid barrier.
 #pragma once
 
 #include "common.cuh"
@@ -114,6 +115,28 @@ __device__ __forceinline__ void aligned_body(const uint32_t *base, uint64_t lo, 
   if (v1 < v0) v1 = v0;
 }
 
+// Streams [0, n) of array `src` (16-byte aligned from element h to element
+// e; plain loads outside) through `f(j, value)` for every element j, one
+// 16-byte load per thread per step: latency is hidden by running up to 64
+// warps per SM (the kernel stays within 32 registers), not by unrolling.
+// Threads `tt` of `ns`.
+template <class F>
+__device__ __forceinline__ void stream_elems(const uint32_t *src, uint32_t n, uint32_t h,
+                                             uint32_t e, uint32_t tt, uint32_t ns, F f) {
+  for (uint32_t j = tt; j < h; j += ns) f(j, __ldg(src + j));
+  for (uint32_t j = e + tt; j < n; j += ns) f(j, __ldg(src + j));
+  const uint4 *s4 = reinterpret_cast<const uint4 *>(src + h);  // 16-byte aligned
+  const uint32_t n4 = (e - h) / 4;
+  for (uint32_t u0 = tt; u0 < n4; u0 += ns) {
+    const uint4 x = __ldcs(s4 + u0);
+    const uint32_t j = h + 4 * u0;
+    f(j, x.x);
+    f(j + 1, x.y);
+    f(j + 2, x.z);
+    f(j + 3, x.w);
+  }
+}
+
 // Grid-wide barrier for a cooperatively launched grid: every CTA adds one to
 // *arrived, and waits (polling with back-off, bounded) until it reaches
 // `target`.  Returns false after recording a timeout.  Call from all threads.
@@ -140,8 +163,8 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *arrived, uint32_t target,
   return s_ok != 0;
 }
 
-template <int NT, int TA, int VW, bool MAT>
-__global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
+template <int NT, int TA, int VW, int MINB, bool MAT>
+__global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
   using Cfg = TileCfg<NT, TA, VW, MAT>;
   constexpr uint32_t SPAN = Cfg::kSpan;
   constexpr int NW = NT / 32;
@@ -150,7 +173,6 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
   uint32_t *tab = smem;                  // T (dense) or the sorted A tile (sparse)
   uint32_t *mbits = smem + Cfg::kTabWords;
 
-  __shared__ uint32_t s_tile, s_w, s_alast;
   __shared__ unsigned long long s_b0, s_b1;
   __shared__ uint32_t warp_sums[NW];
   __shared__ unsigned long long red[NW];
@@ -166,144 +188,111 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
     uint64_t tn = na; na = nb; nb = tn;
   }
   if (skip_by_rule(p.skip_rule, p.ratio_thr, na, nb)) return;
-  const uint64_t ntiles = nb ? (na + TA - 1) / TA : 0;  // no B: nothing to match
   const uint32_t G = gridDim.x;
+  // this CTA's run of A (empty when B is)
+  const uint64_t ca0 = nb ? uint64_t(blockIdx.x) * na / G : 0;
+  const uint64_t ca1 = nb ? (uint64_t(blockIdx.x) + 1) * na / G : 0;
   // B's first and last values guide the searches (uniformly spread values
   // land close to the guess)
   const uint32_t bfirst = nb ? __ldg(B) : 0u, blast = nb ? __ldg(B + nb - 1) : 0u;
+  auto guess = [&](uint32_t key) -> uint64_t {
+    if (blast <= bfirst || key <= bfirst) return 0;
+    return uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
+  };
 
   for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords) / 4; i += NT)
     reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
 
-  uint32_t cnt = 0;  // count mode
-  for (;;) {
-    if (t == 0) s_tile = atomicAdd(&p.sync->ticket, 1u);
-    __syncthreads();  // also: the last tile's T / M use is over
-    const uint32_t tile = s_tile;
-    if (uint64_t(tile) >= ntiles) break;
-    const uint64_t i0 = uint64_t(tile) * TA;
-    const uint64_t i1 = (i0 + TA < na) ? i0 + TA : na;
+  uint32_t cnt = 0;       // count mode
+  uint64_t staged = 0;    // materialise: matches staged so far (at ca0)
+  uint64_t b_next = 0;    // B range start of the next tile
+  for (uint64_t i0 = ca0; i0 < ca1; i0 += TA) {
+    const uint64_t i1 = (i0 + TA < ca1) ? i0 + TA : ca1;
     const uint32_t ntile = uint32_t(i1 - i0);
+    const bool first = i0 == ca0;
+    const int searchers = first ? 2 : 1;  // warps searching B this tile
+    const uint32_t w = __ldg(A + i0), alast = __ldg(A + i1 - 1);
+    const bool dense = alast - w < SPAN;
+    const uint32_t span = alast - w;
 
-    // ---- 1. B range (warps 0, 1) and A tile (the other warps) ----
-    if (warp < 2) {
-      const uint32_t w = __ldg(A + i0), alast = __ldg(A + i1 - 1);
-      const uint32_t v = (warp == 0) ? w : alast;
+    // ---- 1. B range (search warps) and A tile (the other warps) ----
+    if (warp < searchers) {
       uint64_t r;
-      if (warp == 1 && alast == 0xffffffffu) {
-        r = nb;
-      } else {
-        const uint32_t key = (warp == 0) ? v : v + 1u;  // [b0, b1): values in [w, alast]
-        uint64_t est = 0;
-        if (blast > bfirst && key > bfirst)
-          est = uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
-        r = warp_lower_bound(B, nb, key, est);
-      }
-      if (lane == 0) {
-        if (warp == 0) {
-          s_b0 = r;
-          s_w = w;
-        } else {
-          s_b1 = r;
-          s_alast = alast;
-        }
+      if (warp == 0) {  // b1: first B value above alast
+        r = (alast == 0xffffffffu) ? nb : warp_lower_bound(B, nb, alast + 1u, guess(alast + 1u));
+        if (lane == 0) s_b1 = r;
+      } else {          // b0 of the CTA's first tile
+        r = warp_lower_bound(B, nb, w, guess(w));
+        if (lane == 0) s_b0 = r;
       }
     } else {
-      const uint32_t w = __ldg(A + i0), alast = __ldg(A + i1 - 1);
-      const bool dense = alast - w < SPAN;
-      const int tt = t - 64;  // 0 .. NT-65
-      constexpr int NS = NT - 64;
-      // aligned body [v0, v1) by 16-byte loads; the ragged ends by plain loads
+      const uint32_t tt = uint32_t(t - 32 * searchers);
+      const uint32_t ns = uint32_t(NT - 32 * searchers);
       uint64_t v0, v1;
       aligned_body(A, i0, i1, v0, v1);
-      auto put = [&](uint64_t i, uint32_t x) {
-        if (dense) {
+      const uint32_t h = uint32_t(v0 - i0), e = uint32_t(v1 - i0);  // tile-relative
+      if (dense) {
+        stream_elems(A + i0, ntile, h, e, tt, ns, [&](uint32_t, uint32_t x) {
           const uint32_t o = x - w;
           atomicOr(&tab[o >> 5], 1u << (o & 31));
-        } else {
-          tab[i - i0] = x;
-        }
-      };
-      if (v0 < v1) {
-        for (uint64_t i = i0 + uint64_t(tt); i < v0; i += NS) put(i, __ldg(A + i));
-        for (uint64_t i = v1 + uint64_t(tt); i < i1; i += NS) put(i, __ldg(A + i));
-        for (uint64_t i = v0 + 4 * uint64_t(tt); i < v1; i += 4 * uint64_t(NS)) {
-          const uint4 x = __ldcs(reinterpret_cast<const uint4 *>(A + i));
-          put(i, x.x);
-          put(i + 1, x.y);
-          put(i + 2, x.z);
-          put(i + 3, x.w);
-        }
+        });
       } else {
-        for (uint64_t i = i0 + uint64_t(tt); i < i1; i += NS) put(i, __ldg(A + i));
+        stream_elems(A + i0, ntile, h, e, tt, ns, [&](uint32_t j, uint32_t x) { tab[j] = x; });
       }
     }
     __syncthreads();
-    const uint32_t w = s_w, alast = s_alast;
-    const bool dense = alast - w < SPAN;
-    const uint32_t span = alast - w;
-    const uint64_t b0 = s_b0, b1 = s_b1 > s_b0 ? s_b1 : s_b0;
+    const uint64_t b0 = first ? s_b0 : b_next;
+    const uint64_t b1 = s_b1 > b0 ? s_b1 : b0;
+    b_next = b1;
 
     // ---- 2. probe B[b0, b1) ----
-    auto probe = [&](uint32_t x) {
-      bool hit;
-      uint32_t pos;  // M bit: value offset (dense) or A position (sparse)
-      if (dense) {
-        pos = x - w;  // <= span: x is in [w, alast]
-        hit = (tab[pos >> 5] >> (pos & 31)) & 1u;
-      } else {
-        uint32_t lo = 0, len = ntile;
-        while (len > 0) {
-          const uint32_t h = len >> 1;
-          if (tab[lo + h] < x) {
-            lo += h + 1;
-            len -= h + 1;
-          } else {
-            len = h;
-          }
-        }
-        pos = lo;
-        hit = lo < ntile && tab[lo] == x;
-      }
-      if (hit) {
-        if (MAT) atomicOr(&mbits[pos >> 5], 1u << (pos & 31));
-        else ++cnt;
-      }
-    };
     {
       uint64_t v0, v1;
       aligned_body(B, b0, b1, v0, v1);
-      if (v0 < v1) {
-        for (uint64_t i = b0 + uint64_t(t); i < v0; i += NT) probe(__ldg(B + i));
-        for (uint64_t i = v1 + uint64_t(t); i < b1; i += NT) probe(__ldg(B + i));
-        const uint4 *B4 = reinterpret_cast<const uint4 *>(B + v0);  // 16-byte aligned
-        const uint64_t n4 = (v1 - v0) / 4;
-        uint64_t u = uint64_t(t);
-        for (; u + NT < n4; u += 2 * NT) {  // two loads in flight
-          const uint4 x = __ldcs(B4 + u), y = __ldcs(B4 + u + NT);
-          probe(x.x); probe(x.y); probe(x.z); probe(x.w);
-          probe(y.x); probe(y.y); probe(y.z); probe(y.w);
-        }
-        if (u < n4) {
-          const uint4 x = __ldcs(B4 + u);
-          probe(x.x); probe(x.y); probe(x.z); probe(x.w);
-        }
+      const uint32_t nbt = uint32_t(b1 - b0);
+      const uint32_t h = uint32_t(v0 - b0), e = uint32_t(v1 - b0);  // relative to b0
+      if (dense) {
+        // every B element here lies in [w, alast]: its bit is in T (the
+        // clamp only guards T's bounds)
+        stream_elems(B + b0, nbt, h, e, uint32_t(t), uint32_t(NT), [&](uint32_t, uint32_t x) {
+          uint32_t pos = x - w;
+          pos = pos <= span ? pos : span + 1;
+          if ((tab[pos >> 5] >> (pos & 31)) & 1u) {
+            if (MAT) atomicOr(&mbits[pos >> 5], 1u << (pos & 31));
+            else ++cnt;
+          }
+        });
       } else {
-        for (uint64_t i = b0 + uint64_t(t); i < b1; i += NT) probe(__ldg(B + i));
+        stream_elems(B + b0, nbt, h, e, uint32_t(t), uint32_t(NT), [&](uint32_t, uint32_t x) {
+          uint32_t lo = 0, len = ntile;
+          while (len > 0) {
+            const uint32_t hh = len >> 1;
+            if (tab[lo + hh] < x) {
+              lo += hh + 1;
+              len -= hh + 1;
+            } else {
+              len = hh;
+            }
+          }
+          if (lo < ntile && tab[lo] == x) {  // M bit by A position
+            if (MAT) atomicOr(&mbits[lo >> 5], 1u << (lo & 31));
+            else ++cnt;
+          }
+        });
       }
     }
     __syncthreads();
 
-    // ---- 3. output (materialise): M in order -> staging at i0 ----
-    const uint32_t mw = dense ? (span >> 5) + 1 : (ntile + 31) / 32;  // M words in use
+    // ---- 3. output (materialise): M in order, appended to the staging run ----
     if (MAT) {
+      const uint32_t mw = dense ? (span >> 5) + 1 : (ntile + 31) / 32;  // M words in use
       // thread t owns M words [t*per, t*per + per)
       const uint32_t per = (mw + NT - 1) / NT;
       const uint32_t m0 = uint32_t(t) * per;
       const uint32_t m1 = (m0 + per < mw) ? m0 + per : mw;
       uint32_t pc = 0;
       for (uint32_t i = m0; i < m1; ++i) pc += __popc(mbits[i]);
-      // block scan of pc
       uint32_t incl = pc;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -315,11 +304,11 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
       uint32_t before = 0, tot = 0;
 #pragma unroll
       for (int k = 0; k < NW; ++k) {
-        const uint32_t s = warp_sums[k];
-        before += (k < warp) ? s : 0u;
-        tot += s;
+        const uint32_t sm = warp_sums[k];
+        before += (k < warp) ? sm : 0u;
+        tot += sm;
       }
-      uint64_t q = i0 + before + incl - pc;
+      uint64_t q = ca0 + staged + before + incl - pc;
       for (uint32_t i = m0; i < m1; ++i) {
         uint32_t m = mbits[i];
         if (!m) continue;
@@ -330,16 +319,16 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
           p.stage[q++] = dense ? w + pos : tab[pos];
         }
       }
-      if (t == 0) p.status[tile] = tot;  // read after the grid barrier
+      staged += tot;
+      __syncthreads();  // sparse: the A tile was read above; warp sums reused
     }
-    // clear T for the next tile (dense: the words used; sparse: the tile,
-    // which the output step above may still be reading)
-    if (MAT && !dense) __syncthreads();
+    // clear T for the next tile (dense: the words used; sparse: the tile)
     {
       const uint32_t tw = dense ? (span >> 5) + 1 : ntile;
       for (uint32_t i = 4u * uint32_t(t); i < tw; i += 4u * NT)
         *reinterpret_cast<uint4 *>(tab + i) = make_uint4(0, 0, 0, 0);
     }
+    __syncthreads();  // T clear before the next tile's insertion
   }
 
   // ---- combine ----
@@ -350,9 +339,9 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (t == 0) {
-      unsigned long long s = 0;
-      for (int k = 0; k < NW; ++k) s += red[k];
-      if (s) atomicAdd(&p.sync->acc, s);
+      unsigned long long sm = 0;
+      for (int k = 0; k < NW; ++k) sm += red[k];
+      if (sm) atomicAdd(&p.sync->acc, sm);
       __threadfence();
       const uint32_t prev = atomicAdd(&p.sync->done, 1u);
       if (prev == G - 1) {
@@ -365,48 +354,26 @@ __global__ void __launch_bounds__(NT) tile_kernel(const MergeArgs p) {
     return;
   }
 
-  // Materialise: place the tiles.  The launch is cooperative, so all CTAs
-  // are resident and grid-wide barriers are safe.  After every tile is
-  // staged (barrier 1), CTA c sums the counts of the contiguous block of
-  // tiles [c*K, c*K + K) and publishes the block total; after barrier 2 it
-  // adds up the totals of blocks 0..c-1 -- plain loads, nothing to wait
-  // for -- and copies its tiles' staged matches to their offsets.
+  // Materialise: publish this CTA's count; after the grid barrier (all CTAs
+  // are resident: cooperative launch) add up the counts of CTAs 0..c-1 --
+  // plain loads, nothing to wait for -- and copy the staged run.
+  if (t == 0) p.coranks[blockIdx.x] = staged;
   if (!grid_barrier(&p.sync->done, G, p.err)) return;
-  const uint32_t nt32 = uint32_t(ntiles);
-  const uint32_t K = (nt32 + G - 1) / G;
-  const uint32_t r0 = (blockIdx.x * K < nt32) ? blockIdx.x * K : nt32;
-  const uint32_t r1 = (r0 + K < nt32) ? r0 + K : nt32;
-  auto block_sum = [&](uint64_t v) -> uint64_t {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    uint64_t s = 0;
-#pragma unroll
-    for (int q = 0; q < NW; ++q) s += red[q];
-    __syncthreads();  // red is reused
-    return s;
-  };
-  uint64_t mine = 0;
-  for (uint32_t j = r0 + uint32_t(t); j < r1; j += NT) mine += p.status[j];
-  const uint64_t block_total = block_sum(mine);
-  if (t == 0) p.coranks[blockIdx.x] = block_total;
-  if (!grid_barrier(&p.sync->done, 2 * G, p.err)) return;
   uint64_t before = 0;
   for (uint32_t c = uint32_t(t); c < blockIdx.x; c += NT) before += p.coranks[c];
-  const uint64_t ex = block_sum(before);
-  if (ex + block_total > p.out_cap) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+  if (lane == 0) red[warp] = before;
+  __syncthreads();
+  uint64_t ex = 0;
+#pragma unroll
+  for (int k = 0; k < NW; ++k) ex += red[k];
+  if (ex + staged > p.out_cap) {
     if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
   } else {
-    uint64_t off = ex;
-    for (uint32_t j = r0; j < r1; ++j) {
-      const uint32_t ck = uint32_t(p.status[j]);  // the same word for every thread
-      const uint32_t *src = p.stage + uint64_t(j) * TA;
-      for (uint32_t q = uint32_t(t); q < ck; q += NT) p.out[off + q] = src[q];
-      off += ck;
-    }
-    // the last block's end is the total
-    if (blockIdx.x == G - 1 && t == 0) *p.out_len = ex + block_total;
+    for (uint64_t q = uint64_t(t); q < staged; q += NT) p.out[ex + q] = p.stage[ca0 + q];
+    // the last CTA's end is the total
+    if (blockIdx.x == G - 1 && t == 0) *p.out_len = ex + staged;
   }
   // the last CTA out resets the coordination words for the next launch
   if (t == 0) {
