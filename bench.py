@@ -14,7 +14,8 @@ policy picks for its size ratio.
 * ``e2e``: the same through the host-pointer C-ABI call
   (``setops_gpu_intersect(..., SETOPS_HOST)``): pinned host inputs copied in
   and the result copied out inside the timed region.
-* ``roofline``: the merge-path kernel on the 2^24 x 2^24 pair; algorithmic
+* ``roofline``: the kernel the policy picks for the 2^24 x 2^24 pair (the
+  tiled bitmap kernel); algorithmic
   bytes = both inputs read + output written, over its CUDA-event time.
 * ``cpu_baseline``: the reference's CPU path (oracle port: best of
   shuffling / SIMD galloping / bmiss per pair) on this host's cores.
@@ -294,7 +295,7 @@ def read_peak():
 def read_traffic():
     """DRAM bytes per launch of the headline kernel from the committed ncu
     summary (profiles/), or None."""
-    f = ROOT / "profiles" / "merge_2e24x2e24_ncu.md"
+    f = ROOT / "profiles" / "bitmap_2e24x2e24_ncu.md"
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read_text())
@@ -398,7 +399,7 @@ def run_gb300(args):
         el_s = float(t.item())
     value = world * len(pairs) * args.steps / el_s
 
-    # roofline: headline merge kernel (the 2^24 x 2^24 pair)
+    # roofline: the headline kernel (the 2^24 x 2^24 pair; size ratio 1 -> tiled bitmap)
     head = max(range(len(pairs)), key=lambda i: pairs[i][0].size)
     s_h, l_h = pairs[head]
     nout = int(SELECTIVITY * s_h.size)
@@ -409,7 +410,7 @@ def run_gb300(args):
     traffic = read_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "merge_kernel (2^24 x 2^24 pair, materialise)",
+                "kernel": "tile_kernel (bitmap; 2^24 x 2^24 pair, materialise)",
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "launch_ms_mean": head_ms, "peak_source": f"{peak_kind} (hbm_gbs)"}
     sweep = []
