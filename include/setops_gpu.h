@@ -164,6 +164,45 @@ int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
                          const size_t *lens, size_t k, uint64_t *count,
                          unsigned flags);
 
+/* ---- batched 2-set --------------------------------------------------------
+ * Many independent pairs in one launch.  Replaces a loop of Intersect2 /
+ * Intersect2C calls over a dataset's pairs (setops/src/intersect.rs:40-41;
+ * the benchmark's per-pair loop, benchmark/src/timer/harness.rs:35-97).  All
+ * sets live in one pool: pair p is pool[a_off[p], +a_len[p]) and
+ * pool[b_off[p], +b_len[p]), each strictly increasing.  The intersection of
+ * pair p (as naive_merge, setops/src/intersect/merge.rs:7-33) goes to
+ * out[out_off[p], +min(a_len[p], b_len[p])) and its length to out_lens[p].
+ * out_off == NULL: the offsets are the running sum of min(a_len, b_len)
+ * (then out_cap must cover that sum; otherwise SETOPS_ERR_CAPACITY).  With
+ * caller offsets on the device the regions are the caller's responsibility.
+ * flags: SETOPS_HOST = every array is host memory.  The kernel shape and the
+ * size ratio from which a pair takes the search path instead of the tile
+ * path come from the batch policy (setops_gpu_batch_set_policy, or the
+ * autotuner).  The calls return when the batch is done. */
+int setops_gpu_batch_intersect(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                               const uint64_t *a_off, const uint64_t *a_len,
+                               const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                               uint32_t *out, size_t out_cap, const uint64_t *out_off,
+                               uint64_t *out_lens, unsigned flags);
+/* Counter visitor per pair (setops/src/visitor.rs:24-49): counts[p]. */
+int setops_gpu_batch_count(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                           const uint64_t *a_off, const uint64_t *a_len, const uint64_t *b_off,
+                           const uint64_t *b_len, size_t npairs, uint64_t *counts,
+                           unsigned flags);
+/* Batch policy: kernel shape (0 .. setops_gpu_batch_num_variants()-1) and
+ * search ratio (pairs with max/min >= ratio take the search path; 0 = never). */
+int setops_gpu_batch_set_policy(setops_ctx *ctx, int variant, uint32_t search_ratio);
+int setops_gpu_batch_get_policy(const setops_ctx *ctx, int *variant, uint32_t *search_ratio);
+int setops_gpu_batch_num_variants(void);
+/* Autotuner: times every kernel shape with several search ratios on the
+ * given sample batch (materialising, `reps` timed runs each) and keeps the
+ * fastest as the batch policy.  Plays the role of the reference's per-ISA
+ * choice of algorithm (setops/src/intersect.rs:26-36). */
+int setops_gpu_batch_autotune(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                              const uint64_t *a_off, const uint64_t *a_len,
+                              const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                              int reps, unsigned flags);
+
 /* ---- 2-set without allocation ----------------------------------------------
  * No counterpart in the reference: it exists for callers of this library that
  * cannot allocate device memory -- a host program that owns all device

@@ -42,6 +42,7 @@ __all__ = [
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
+    "batch_intersect", "batch_count", "batch_autotune",
 ]
 
 
@@ -266,6 +267,62 @@ class UnsafeWriter(SliceWriter):
 
     def into(self) -> np.ndarray:
         return self.as_array().copy()
+
+
+# ---------------------------------------------------------------------------
+# batched pairs (many pairs, one launch)
+
+def _u64(x) -> np.ndarray:
+    return np.ascontiguousarray(x, dtype=np.uint64)
+
+
+def batch_intersect(pool, a_off, a_len, b_off, b_len, *, ctx: Context | None = None):
+    """Intersects every pair of a batch in one launch (host arrays).  Pair p
+    is pool[a_off[p]:+a_len[p]] and pool[b_off[p]:+b_len[p]].  Returns
+    (out, out_off, out_lens): pair p's ascending intersection is
+    out[out_off[p]:out_off[p] + out_lens[p]]."""
+    ctx = ctx or default_context()
+    pool = np.ascontiguousarray(pool, dtype=np.uint32)
+    a_off, a_len, b_off, b_len = _u64(a_off), _u64(a_len), _u64(b_off), _u64(b_len)
+    n = a_len.size
+    caps = np.minimum(a_len, b_len)
+    out_off = np.zeros(n, np.uint64)
+    if n:
+        out_off[1:] = np.cumsum(caps[:-1])
+    out = np.empty(max(int(caps.sum()), 1), np.uint32)
+    lens = np.zeros(n, np.uint64)
+    ctx.check(lib.setops_gpu_batch_intersect(
+        ctx.handle, pool.ctypes.data, pool.size, a_off.ctypes.data, a_len.ctypes.data,
+        b_off.ctypes.data, b_len.ctypes.data, n, out.ctypes.data, out.size,
+        out_off.ctypes.data, lens.ctypes.data, HOST))
+    return out, out_off, lens
+
+
+def batch_count(pool, a_off, a_len, b_off, b_len, *, ctx: Context | None = None) -> np.ndarray:
+    """Per-pair |A ∩ B| of a batch in one launch (host arrays)."""
+    ctx = ctx or default_context()
+    pool = np.ascontiguousarray(pool, dtype=np.uint32)
+    a_off, a_len, b_off, b_len = _u64(a_off), _u64(a_len), _u64(b_off), _u64(b_len)
+    counts = np.zeros(a_len.size, np.uint64)
+    ctx.check(lib.setops_gpu_batch_count(
+        ctx.handle, pool.ctypes.data, pool.size, a_off.ctypes.data, a_len.ctypes.data,
+        b_off.ctypes.data, b_len.ctypes.data, a_len.size, counts.ctypes.data, HOST))
+    return counts
+
+
+def batch_autotune(pool, a_off, a_len, b_off, b_len, *, reps: int = 3,
+                   ctx: Context | None = None) -> tuple[int, int]:
+    """Times the batch kernel shapes and search ratios on a sample batch and
+    keeps the fastest as the context's batch policy; returns it."""
+    ctx = ctx or default_context()
+    pool = np.ascontiguousarray(pool, dtype=np.uint32)
+    a_off, a_len, b_off, b_len = _u64(a_off), _u64(a_len), _u64(b_off), _u64(b_len)
+    ctx.check(lib.setops_gpu_batch_autotune(
+        ctx.handle, pool.ctypes.data, pool.size, a_off.ctypes.data, a_len.ctypes.data,
+        b_off.ctypes.data, b_len.ctypes.data, a_len.size, reps, HOST))
+    v, r = C.c_int(), C.c_uint32()
+    ctx.check(lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v), C.byref(r)))
+    return int(v.value), int(r.value)
 
 
 # ---------------------------------------------------------------------------

@@ -78,6 +78,12 @@ SIGNATURES = [
     ("setops_gpu_svs_count", C.c_int, [vp, C.POINTER(vp), szp, sz, u64p, uint]),
     ("setops_gpu_validate_sorted", C.c_int, [vp, vp, sz, C.POINTER(C.c_int), uint]),
     ("setops_gpu_intersect_noalloc", C.c_int, [vp, sz, vp, sz, vp, sz, szp, vp]),
+    ("setops_gpu_batch_intersect", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, sz, vp, vp, uint]),
+    ("setops_gpu_batch_count", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, uint]),
+    ("setops_gpu_batch_set_policy", C.c_int, [vp, C.c_int, C.c_uint32]),
+    ("setops_gpu_batch_get_policy", C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
+    ("setops_gpu_batch_num_variants", C.c_int, []),
+    ("setops_gpu_batch_autotune", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, C.c_int, uint]),
     # setops_bench.h
     ("setops_gen_twoset", C.c_int, [u64, C.c_double, C.c_double, sz, sz, vp, vp]),
     ("setops_gen_kset_lens", C.c_int, [sz, C.c_double, sz, szp]),

@@ -68,6 +68,8 @@ struct setops_ctx {
   uint64_t launches = 0;
   std::map<const void *, int> occ;
   unsigned policy[2][setops::kRatioBands] = {};
+  int batch_variant = 0;             // batch kernel shape
+  uint32_t batch_search_ratio = 16;  // batch pairs with max/min >= this: search path
 
   std::vector<setops::DevBuf *> all_bufs() {
     std::vector<setops::DevBuf *> v = {&status, &out0, &out1, &stage0,

@@ -110,7 +110,8 @@ __device__ __forceinline__ void aligned_body(const uint32_t *base, uint64_t lo, 
                                              uint64_t &v0, uint64_t &v1) {
   const uint64_t mis = (reinterpret_cast<uintptr_t>(base) >> 2) & 3;  // words past 16 B
   v0 = lo + ((4 - ((mis + lo) & 3)) & 3);
-  v1 = hi - ((mis + hi) & 3);
+  const uint64_t r = (mis + hi) & 3;
+  v1 = hi >= r ? hi - r : 0;  // (unsigned: never below zero)
   if (v0 > hi) v0 = hi;
   if (v1 < v0) v1 = v0;
 }
@@ -163,55 +164,48 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *arrived, uint32_t target,
   return s_ok != 0;
 }
 
-template <int NT, int TA, int VW, int MINB, bool MAT>
-__global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
+// Shared-memory words of one CTA used by tile_run.
+template <int NT>
+struct TileShared {
+  unsigned long long b0, b1;
+  uint32_t warp_sums[NT / 32];
+};
+
+// Intersects the run A[i_begin, i_end) of a sorted set with the sorted set
+// B[0, nb), tile by tile (see the file comment).  `search`: find each tile's
+// B range by warp searches (B is long and the run covers part of it); else
+// every tile probes all of B (a short B, e.g. a pair that fits one tile).
+// T and M (tab, mbits) must be zero on entry; they are zero again on return.
+// Materialise: appends the matches in ascending order at dst[0, ...) and
+// returns their number (the same in every thread).  Count mode: returns this
+// thread's share of the count (the caller sums over the CTA).  All NT
+// threads call it.
+template <int NT, int TA, int VW, bool MAT>
+__device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin,
+                                             uint64_t i_end, const uint32_t *B, uint64_t nb,
+                                             bool search, uint32_t *dst, uint32_t *tab,
+                                             uint32_t *mbits, TileShared<NT> &sh) {
   using Cfg = TileCfg<NT, TA, VW, MAT>;
   constexpr uint32_t SPAN = Cfg::kSpan;
   constexpr int NW = NT / 32;
-
-  extern __shared__ __align__(128) uint32_t smem[];
-  uint32_t *tab = smem;                  // T (dense) or the sorted A tile (sparse)
-  uint32_t *mbits = smem + Cfg::kTabWords;
-
-  __shared__ unsigned long long s_b0, s_b1;
-  __shared__ uint32_t warp_sums[NW];
-  __shared__ unsigned long long red[NW];
-
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-
-  // ---- problem (A = smaller set) ----
-  uint64_t na = p.na_dev ? *p.na_dev : p.na;
-  uint64_t nb = p.nb_dev ? *p.nb_dev : p.nb;
-  const uint32_t *A = p.a, *B = p.b;
-  if (na > nb) {
-    const uint32_t *tp = A; A = B; B = tp;
-    uint64_t tn = na; na = nb; nb = tn;
-  }
-  if (skip_by_rule(p.skip_rule, p.ratio_thr, na, nb)) return;
-  const uint32_t G = gridDim.x;
-  // this CTA's run of A (empty when B is)
-  const uint64_t ca0 = nb ? uint64_t(blockIdx.x) * na / G : 0;
-  const uint64_t ca1 = nb ? (uint64_t(blockIdx.x) + 1) * na / G : 0;
   // B's first and last values guide the searches (uniformly spread values
   // land close to the guess)
-  const uint32_t bfirst = nb ? __ldg(B) : 0u, blast = nb ? __ldg(B + nb - 1) : 0u;
+  const uint32_t bfirst = (search && nb) ? __ldg(B) : 0u;
+  const uint32_t blast = (search && nb) ? __ldg(B + nb - 1) : 0u;
   auto guess = [&](uint32_t key) -> uint64_t {
     if (blast <= bfirst || key <= bfirst) return 0;
     return uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
   };
-
-  for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords) / 4; i += NT)
-    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
-  __syncthreads();
-
   uint32_t cnt = 0;       // count mode
-  uint64_t staged = 0;    // materialise: matches staged so far (at ca0)
+  uint64_t staged = 0;    // materialise: matches written so far
   uint64_t b_next = 0;    // B range start of the next tile
-  for (uint64_t i0 = ca0; i0 < ca1; i0 += TA) {
-    const uint64_t i1 = (i0 + TA < ca1) ? i0 + TA : ca1;
+  for (uint64_t i0 = i_begin; i0 < i_end; i0 += TA) {
+    const uint64_t i1 = (i0 + TA < i_end) ? i0 + TA : i_end;
     const uint32_t ntile = uint32_t(i1 - i0);
-    const bool first = i0 == ca0;
-    const int searchers = first ? 2 : 1;  // warps searching B this tile
+    const bool first = i0 == i_begin;
+    // warps searching B this tile (none when B is probed whole)
+    const int searchers = !search ? 0 : (first ? 2 : 1);
     const uint32_t w = __ldg(A + i0), alast = __ldg(A + i1 - 1);
     const bool dense = alast - w < SPAN;
     const uint32_t span = alast - w;
@@ -221,10 +215,10 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
       uint64_t r;
       if (warp == 0) {  // b1: first B value above alast
         r = (alast == 0xffffffffu) ? nb : warp_lower_bound(B, nb, alast + 1u, guess(alast + 1u));
-        if (lane == 0) s_b1 = r;
+        if (lane == 0) sh.b1 = r;
       } else {          // b0 of the CTA's first tile
         r = warp_lower_bound(B, nb, w, guess(w));
-        if (lane == 0) s_b0 = r;
+        if (lane == 0) sh.b0 = r;
       }
     } else {
       const uint32_t tt = uint32_t(t - 32 * searchers);
@@ -242,8 +236,8 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
       }
     }
     __syncthreads();
-    const uint64_t b0 = first ? s_b0 : b_next;
-    const uint64_t b1 = s_b1 > b0 ? s_b1 : b0;
+    const uint64_t b0 = !search ? 0 : (first ? uint64_t(sh.b0) : b_next);
+    const uint64_t b1 = !search ? nb : (sh.b1 > b0 ? uint64_t(sh.b1) : b0);
     b_next = b1;
 
     // ---- 2. probe B[b0, b1) ----
@@ -299,16 +293,16 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
       }
-      if (lane == 31) warp_sums[warp] = incl;
+      if (lane == 31) sh.warp_sums[warp] = incl;
       __syncthreads();
       uint32_t before = 0, tot = 0;
 #pragma unroll
       for (int k = 0; k < NW; ++k) {
-        const uint32_t sm = warp_sums[k];
+        const uint32_t sm = sh.warp_sums[k];
         before += (k < warp) ? sm : 0u;
         tot += sm;
       }
-      uint64_t q = ca0 + staged + before + incl - pc;
+      uint64_t q = staged + before + incl - pc;
       for (uint32_t i = m0; i < m1; ++i) {
         uint32_t m = mbits[i];
         if (!m) continue;
@@ -316,7 +310,7 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
         while (m) {
           const uint32_t pos = i * 32u + uint32_t(__ffs(m) - 1);
           m &= m - 1;
-          p.stage[q++] = dense ? w + pos : tab[pos];
+          dst[q++] = dense ? w + pos : tab[pos];
         }
       }
       staged += tot;
@@ -330,6 +324,46 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
     }
     __syncthreads();  // T clear before the next tile's insertion
   }
+
+  return MAT ? staged : uint64_t(cnt);
+}
+
+template <int NT, int TA, int VW, int MINB, bool MAT>
+__global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
+  using Cfg = TileCfg<NT, TA, VW, MAT>;
+  constexpr int NW = NT / 32;
+
+  extern __shared__ __align__(128) uint32_t smem[];
+  uint32_t *tab = smem;                  // T (dense) or the sorted A tile (sparse)
+  uint32_t *mbits = smem + Cfg::kTabWords;
+
+  __shared__ TileShared<NT> sh;
+  __shared__ unsigned long long red[NW];
+
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+  // ---- problem (A = smaller set) ----
+  uint64_t na = p.na_dev ? *p.na_dev : p.na;
+  uint64_t nb = p.nb_dev ? *p.nb_dev : p.nb;
+  const uint32_t *A = p.a, *B = p.b;
+  if (na > nb) {
+    const uint32_t *tp = A; A = B; B = tp;
+    uint64_t tn = na; na = nb; nb = tn;
+  }
+  if (skip_by_rule(p.skip_rule, p.ratio_thr, na, nb)) return;
+  const uint32_t G = gridDim.x;
+  // this CTA's run of A (empty when B is)
+  const uint64_t ca0 = nb ? uint64_t(blockIdx.x) * na / G : 0;
+  const uint64_t ca1 = nb ? (uint64_t(blockIdx.x) + 1) * na / G : 0;
+
+  for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords) / 4; i += NT)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  __syncthreads();
+
+  const uint64_t r = tile_run<NT, TA, VW, MAT>(A, ca0, ca1, B, nb, true, p.stage + ca0, tab,
+                                                mbits, sh);
+  const uint32_t cnt = MAT ? 0u : uint32_t(r);
+  const uint64_t staged = MAT ? r : 0;
 
   // ---- combine ----
   if (!MAT) {
@@ -354,36 +388,38 @@ __global__ void __launch_bounds__(NT, MINB) tile_kernel(const MergeArgs p) {
     return;
   }
 
-  // Materialise: publish this CTA's count; after the grid barrier (all CTAs
-  // are resident: cooperative launch) add up the counts of CTAs 0..c-1 --
-  // plain loads, nothing to wait for -- and copy the staged run.
-  if (t == 0) p.coranks[blockIdx.x] = staged;
-  if (!grid_barrier(&p.sync->done, G, p.err)) return;
-  uint64_t before = 0;
-  for (uint32_t c = uint32_t(t); c < blockIdx.x; c += NT) before += p.coranks[c];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
-  if (lane == 0) red[warp] = before;
-  __syncthreads();
-  uint64_t ex = 0;
-#pragma unroll
-  for (int k = 0; k < NW; ++k) ex += red[k];
-  if (ex + staged > p.out_cap) {
-    if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
-  } else {
-    for (uint64_t q = uint64_t(t); q < staged; q += NT) p.out[ex + q] = p.stage[ca0 + q];
-    // the last CTA's end is the total
-    if (blockIdx.x == G - 1 && t == 0) *p.out_len = ex + staged;
-  }
-  // the last CTA out resets the coordination words for the next launch
-  if (t == 0) {
-    __threadfence();
-    const unsigned long long prev = atomicAdd(&p.sync->acc, 1ull);
-    if (prev == G - 1) {
-      p.sync->ticket = 0;
-      p.sync->done = 0;
-      p.sync->acc = 0;
+  if constexpr (MAT) {
+    // Materialise: publish this CTA's count; after the grid barrier (all CTAs
+    // are resident: cooperative launch) add up the counts of CTAs 0..c-1 --
+    // plain loads, nothing to wait for -- and copy the staged run.
+    if (t == 0) p.coranks[blockIdx.x] = staged;
+    if (!grid_barrier(&p.sync->done, G, p.err)) return;
+    uint64_t before = 0;
+    for (uint32_t c = uint32_t(t); c < blockIdx.x; c += NT) before += p.coranks[c];
+  #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) red[warp] = before;
+    __syncthreads();
+    uint64_t ex = 0;
+  #pragma unroll
+    for (int k = 0; k < NW; ++k) ex += red[k];
+    if (ex + staged > p.out_cap) {
+      if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
+    } else {
+      for (uint64_t q = uint64_t(t); q < staged; q += NT) p.out[ex + q] = p.stage[ca0 + q];
+      // the last CTA's end is the total
+      if (blockIdx.x == G - 1 && t == 0) *p.out_len = ex + staged;
+    }
+    // the last CTA out resets the coordination words for the next launch
+    if (t == 0) {
       __threadfence();
+      const unsigned long long prev = atomicAdd(&p.sync->acc, 1ull);
+      if (prev == G - 1) {
+        p.sync->ticket = 0;
+        p.sync->done = 0;
+        p.sync->acc = 0;
+        __threadfence();
+      }
     }
   }
 }

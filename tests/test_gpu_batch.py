@@ -1,0 +1,133 @@
+"""Batched pairs (setops_gpu_batch_intersect / _count): every pair of a batch
+in one launch must equal naive_merge of that pair (the reference's oracle,
+setops/src/intersect/merge.rs:7-33), for every kernel shape and search ratio
+of the batch policy, through host and device arrays."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import rand_set
+
+pytestmark = pytest.mark.gpu
+
+import simd_set_operations_gb300 as so  # noqa: E402
+from simd_set_operations_gb300 import _lib, datasets as ds  # noqa: E402
+
+
+def expected(orc, batch):
+    pairs = [batch.pair(p) for p in range(len(batch))]
+    outs = [np.empty(max(min(a.size, b.size), 1), np.uint32) for a, b in pairs]
+    counts = orc.run_pairs(orc.NAIVE_MERGE, pairs, 8, outs=outs)
+    return [o[:int(c)] for o, c in zip(outs, counts)]
+
+
+def check_batch(ctx, orc, batch, want=None):
+    want = want or expected(orc, batch)
+    out, out_off, lens = so.batch_intersect(batch.pool, batch.a_off, batch.a_len, batch.b_off,
+                                            batch.b_len, ctx=ctx)
+    for p, w in enumerate(want):
+        got = out[int(out_off[p]):int(out_off[p]) + int(lens[p])]
+        assert int(lens[p]) == w.size and np.array_equal(got, w), (p, batch.a_len[p], batch.b_len[p])
+    counts = so.batch_count(batch.pool, batch.a_off, batch.a_len, batch.b_off, batch.b_len, ctx=ctx)
+    assert [int(c) for c in counts] == [w.size for w in want]
+    return want
+
+
+def handmade_batch():
+    """Edge cases: empty sides, identical sets, disjoint, one element, values
+    near 2^32, a pair longer than one tile, and a strongly skewed pair."""
+    rng = np.random.default_rng(7)
+    big = rand_set(rng, 20000, 1 << 20)
+    sets = [
+        (np.empty(0, np.uint32), rand_set(rng, 50, 1000)),
+        (rand_set(rng, 50, 1000), np.empty(0, np.uint32)),
+        (big, big.copy()),
+        (np.arange(0, 1000, 2, dtype=np.uint32), np.arange(1, 1000, 2, dtype=np.uint32)),
+        (np.array([5], np.uint32), np.array([5], np.uint32)),
+        (np.array([0xFFFFFFFF], np.uint32), np.array([0, 7, 0xFFFFFFFE, 0xFFFFFFFF], np.uint32)),
+        (rand_set(rng, 9000, 1 << 16), rand_set(rng, 30000, 1 << 16)),
+        (rand_set(rng, 40, 1 << 30), rand_set(rng, 60000, 1 << 30)),
+    ]
+    pool = np.concatenate([np.concatenate([a, b]) for a, b in sets]).astype(np.uint32)
+    a_off, a_len, b_off, b_len = [], [], [], []
+    off = 0
+    for a, b in sets:
+        a_off.append(off); a_len.append(a.size); off += a.size
+        b_off.append(off); b_len.append(b.size); off += b.size
+    u = lambda x: np.array(x, np.uint64)  # noqa: E731
+    return ds.PairBatch(pool, u(a_off), u(a_len), u(b_off), u(b_len))
+
+
+@pytest.fixture(scope="module")
+def generated():
+    # the reference shape (log-uniform sizes, density and selectivity drawn
+    # per pair), scaled down: 3000 pairs of up to 2^14 elements
+    return ds.gen_batch(20240611, 3000, 16, 1 << 14)
+
+
+def test_batch_generated_every_policy(ctx, orc, generated):
+    want = expected(orc, generated)
+    v0, r0 = C.c_int(), C.c_uint32()
+    ctx.check(_lib.lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v0), C.byref(r0)))
+    try:
+        for v in range(_lib.lib.setops_gpu_batch_num_variants()):
+            for ratio in (0, 1, 8, 64):  # never / always / sometimes the search path
+                ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v, ratio))
+                check_batch(ctx, orc, generated, want)
+    finally:
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))
+
+
+def test_batch_edge_cases(ctx, orc):
+    b = handmade_batch()
+    for ratio in (0, 1, 64):
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, 0, ratio))
+        check_batch(ctx, orc, b)
+    ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, 0, 16))
+
+
+def test_batch_device_arrays_and_offsets(ctx, orc, generated):
+    """Device arrays with the output offsets from the device scan, twice in a
+    row; then a capacity error."""
+    import torch
+    want = expected(orc, generated)
+    t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).view(dt)).cuda()  # noqa: E731
+    pool = t(generated.pool, np.int32)
+    arrs = [t(x, np.int64) for x in (generated.a_off, generated.a_len, generated.b_off,
+                                     generated.b_len)]
+    n = len(generated)
+    cap = int(np.minimum(generated.a_len, generated.b_len).sum())
+    caps = np.minimum(generated.a_len, generated.b_len)
+    offs = np.zeros(n, np.uint64)
+    offs[1:] = np.cumsum(caps[:-1])
+    for _ in range(2):
+        out = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+        lens = torch.zeros(n, dtype=torch.int64, device="cuda")
+        ctx.check(_lib.lib.setops_gpu_batch_intersect(
+            ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+            out.data_ptr(), cap, None, lens.data_ptr(), 0))
+        o = out.cpu().numpy().view(np.uint32)
+        ln = lens.cpu().numpy()
+        for p, w in enumerate(want):
+            lo, n_p = int(offs[p]), int(ln[p])
+            assert n_p == w.size and np.array_equal(o[lo:lo + n_p], w), p
+    rc = _lib.lib.setops_gpu_batch_intersect(
+        ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+        out.data_ptr(), cap - 1, None, lens.data_ptr(), 0)
+    assert rc == _lib.ERR_CAPACITY
+
+
+def test_batch_autotune_keeps_results_exact(ctx, orc, generated):
+    want = expected(orc, generated)
+    v0, r0 = C.c_int(), C.c_uint32()
+    ctx.check(_lib.lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v0), C.byref(r0)))
+    try:
+        v, r = so.batch_autotune(generated.pool, generated.a_off, generated.a_len,
+                                 generated.b_off, generated.b_len, reps=1, ctx=ctx)
+        assert 0 <= v < _lib.lib.setops_gpu_batch_num_variants()
+        check_batch(ctx, orc, generated, want)
+    finally:
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))
