@@ -20,6 +20,10 @@ policy picks for its size ratio.
 * ``cpu_baseline``: the reference's CPU path (oracle port: best of
   shuffling / SIMD galloping / bmiss per pair) on this host's cores.
 
+* ``batch``: the batched configuration -- 100,000 uneven pairs in one
+  persistent launch (policy autotuned on a sample) against one launch per
+  pair on a sample of the same pairs; results checked equal.
+
 ``--impl reference`` times that CPU path alone on all host threads (pairs
 spread over threads), rank 0 only.
 """
@@ -61,6 +65,9 @@ def parse():
     p.add_argument("--min-warmup-seconds", type=float, default=2.0,
                    help="keep warming up at least this long (gives the clock sampler "
                         "load to observe)")
+    p.add_argument("--no-batch", action="store_true",
+                   help="skip the batched-pairs leg (100k uneven pairs in one launch)")
+    p.add_argument("--batch-pairs", type=int, default=100000)
     p.add_argument("--pairs", default="0,1,2,3",
                    help="which sweep pairs to run (profiling subsets; default all)")
     return p.parse_args()
@@ -302,6 +309,103 @@ def read_traffic():
     return int(m.group(1)) if m else None
 
 
+BATCH_SEED = 20240611
+
+
+def batch_leg(ctx, stream, npairs: int) -> dict:
+    """Batched uneven pairs (the reference's batched configuration): npairs
+    pairs with set sizes log-uniform in [2^4, 2^16], per-pair density
+    U[0.01, 0.5] and selectivity U[0, 0.5], intersected in one launch from
+    device-resident data, against the plain path of one launch per pair on a
+    sample of the same pairs.  The batch policy is first autotuned on the
+    first 10,000 pairs.  The per-pair results of the sample must equal the
+    batch's."""
+    import ctypes as C
+
+    import torch
+
+    from simd_set_operations_gb300 import _lib, datasets as ds
+    L = _lib.lib
+    b = ds.gen_batch(BATCH_SEED, npairs, 16, 1 << 16)
+    td = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).view(dt)).cuda()  # noqa: E731
+    pool = td(b.pool, np.int32)
+    arrs = [td(x, np.int64) for x in (b.a_off, b.a_len, b.b_off, b.b_len)]
+    caps = np.minimum(b.a_len, b.b_len)
+    cap = int(caps.sum())
+    offs = np.zeros(npairs, np.uint64)
+    offs[1:] = np.cumsum(caps[:-1])
+    doffs = td(offs, np.int64)
+    out = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    lens = torch.zeros(npairs, dtype=torch.int64, device="cuda")
+    # autotune the batch policy on a sample (device arrays)
+    nt = min(npairs, 10000)
+    ctx.check(L.setops_gpu_batch_autotune(ctx.handle, pool.data_ptr(), pool.numel(),
+                                          *[a.data_ptr() for a in arrs], nt, 3, 0))
+    v, r = C.c_int(), C.c_uint32()
+    ctx.check(L.setops_gpu_batch_get_policy(ctx.handle, C.byref(v), C.byref(r)))
+
+    def run():
+        ctx.check(L.setops_gpu_batch_intersect(
+            ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], npairs,
+            out.data_ptr(), cap, doffs.data_ptr(), lens.data_ptr(), 0))
+
+    for _ in range(2):
+        run()
+    ts = []
+    for _ in range(7):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t_batch = sorted(ts)[len(ts) // 2]
+    matches = int(lens.sum().item())
+    alg = 4 * int(b.pool.size) + 4 * matches
+    # the plain path: one launch per pair (async C-ABI on device pointers)
+    ns = min(npairs, 3000)
+    out2 = torch.empty(max(int(caps[:ns].sum()), 1), dtype=torch.int32, device="cuda")
+    ln2 = torch.zeros(ns, dtype=torch.int64, device="cuda")
+    base, obase, lbase = pool.data_ptr(), out2.data_ptr(), ln2.data_ptr()
+
+    def per_pair():
+        for p in range(ns):
+            rc = L.setops_gpu_intersect_async(
+                ctx.handle, base + 4 * int(b.a_off[p]), int(b.a_len[p]),
+                base + 4 * int(b.b_off[p]), int(b.b_len[p]), obase + 4 * int(offs[p]),
+                int(caps[p]), lbase + 8 * p, 0)
+            if rc != 0:
+                ctx.check(rc)
+        ctx.check(L.setops_gpu_synchronize(ctx.handle))
+
+    per_pair()
+    t0 = time.perf_counter()
+    per_pair()
+    t_pp = time.perf_counter() - t0
+    # exactness: the sample's per-pair results equal the batch's
+    l1, l2 = lens[:ns].cpu().numpy(), ln2.cpu().numpy()
+    o1 = out[:int(caps[:ns].sum())].cpu().numpy()
+    o2 = out2.cpu().numpy()
+    for p in range(ns):
+        lo, n1 = int(offs[p]), int(l1[p])
+        if n1 != int(l2[p]) or not np.array_equal(o1[lo:lo + n1], o2[lo:lo + n1]):
+            raise SystemExit(f"batched result of pair {p} differs from the per-pair path")
+    peak, _ = read_peak()
+    return {
+        "workload": f"{npairs} pairs, sizes log-uniform in [2^4, 2^16] per set, density "
+                    "U[0.01, 0.5], selectivity U[0, 0.5], u32, materialised; inputs resident",
+        "pairs": npairs, "pool_bytes": 4 * int(b.pool.size), "matches": matches,
+        "ms": 1e3 * t_batch, "pairs_per_s": npairs / t_batch,
+        "GBps_algorithmic": alg / t_batch / 1e9, "frac_of_peak": alg / t_batch / 1e9 / peak,
+        "policy": {"variant": int(v.value), "search_ratio": int(r.value),
+                   "tuned_on_pairs": nt},
+        "one_launch_per_pair": {"pairs_per_s": ns / t_pp, "sample_pairs": ns,
+                                "api": "setops_gpu_intersect_async per pair, device pointers"},
+        "speedup_vs_one_launch_per_pair": (npairs / t_batch) / (ns / t_pp),
+        "results_match_per_pair_path": True,
+    }
+
+
 def run_gb300(args):
     import ctypes as C
 
@@ -484,6 +588,10 @@ def run_gb300(args):
                "host_cores": cores, "arch": os.uname().machine,
                "results_match_gpu": True}
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = batch_leg(ctx, stream, args.batch_pairs)
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el_s / args.steps,
@@ -491,7 +599,7 @@ def run_gb300(args):
         "data": "synthetic (seeded; reference generator shape)",
         "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep,
+        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "batch": batch,
         "timing": {"bracket_ms_total": wall_ms, "kernel_ms_total": dev_ms,
                    "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
                            "sync inside); kernel_ms_total sums the per-launch events"},
