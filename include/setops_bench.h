@@ -64,6 +64,21 @@ int setops_gen_index_fill(uint64_t seed, size_t nlists, const uint64_t *lens,
                           const uint64_t *offs, uint64_t doc_space,
                           uint32_t *pool, int nthreads);
 
+/* k-set queries over a posting-list index: k uniform in [kmin, kmax]
+ * (kmax <= 16), then k distinct list ids (0-based popularity ranks) drawn
+ * Zipf(s) over rank.  ids is nq x kmax, row q holding ks[q] ids. */
+int setops_gen_queries(uint64_t seed, size_t nq, size_t nlists, uint32_t kmin,
+                       uint32_t kmax, double s, uint32_t *ids, uint32_t *ks);
+
+/* Open-loop load for a server: query q (ids row q of an nq x kstride array,
+ * ks[q] ids) arrives at the q-th point of a Poisson process of rate
+ * rate_qps; latency_ns[q] runs from that arrival to completion, counts[q]
+ * (optional) is the answer's length.  Returns when every query is done. */
+struct setops_srv;
+int setops_srv_run_load(struct setops_srv *srv, const uint32_t *ids, const uint32_t *ks,
+                        size_t kstride, size_t nq, double rate_qps, uint64_t seed,
+                        uint64_t *latency_ns, uint64_t *counts, double *elapsed_s);
+
 /* Sorted, duplicate-free sample of n values from [0, max_value). */
 int setops_gen_sorted_sample(uint64_t seed, size_t n, uint64_t max_value,
                              uint32_t *out);

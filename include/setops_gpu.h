@@ -203,6 +203,34 @@ int setops_gpu_batch_autotune(setops_ctx *ctx, const uint32_t *pool, size_t pool
                               const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
                               int reps, unsigned flags);
 
+/* ---- serving k-set queries against a resident index ----------------------
+ * No single counterpart in the reference: it serves run_svs / svs_generic
+ * (setops/src/intersect/svs.rs:50-73,103-116) over a posting-list index, the
+ * way a search engine would call it, with continuous batching.  The index is
+ * a pool of sorted lists: list i is pool[offs[i], +lens[i]) (flags
+ * SETOPS_HOST: host arrays, copied to the device; else device arrays, which
+ * must outlive the server).  A query names k in [2, 16] list ids; its answer
+ * is their ascending intersection (svs_generic with naive_merge semantics).
+ * A server thread admits waiting queries into batches while their scratch
+ * fits `scratch_budget` bytes (0: 256 MiB) and keeps up to two batches on
+ * the GPU at once; queries arriving while a batch runs join the next one.
+ * submit is non-blocking and thread-safe; poll returns one finished query
+ * (tag, answer, latency from submit to completion) or SETOPS_ERR_NOT_READY;
+ * SETOPS_ERR_CAPACITY leaves the answer queued and sets *out_len to its
+ * size.  The server uses the context's device and batch policy; do not run
+ * other calls on the same context concurrently with a server. */
+typedef struct setops_srv setops_srv;
+int setops_srv_start(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                     const uint64_t *offs, const uint64_t *lens, size_t nlists,
+                     size_t scratch_budget, unsigned flags, setops_srv **out);
+int setops_srv_submit(setops_srv *srv, const uint32_t *list_ids, size_t k, uint64_t tag);
+int setops_srv_poll(setops_srv *srv, uint64_t *tag, uint32_t *out, size_t out_cap,
+                    size_t *out_len, uint64_t *latency_ns);
+int setops_srv_stats(setops_srv *srv, uint64_t *batches, uint64_t *queries,
+                     uint64_t *max_batch, uint64_t *launches);
+/* Waits for every submitted query, stops the thread, frees the server. */
+int setops_srv_stop(setops_srv *srv);
+
 /* ---- 2-set without allocation ----------------------------------------------
  * No counterpart in the reference: it exists for callers of this library that
  * cannot allocate device memory -- a host program that owns all device

@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import ctypes as C
 import threading
+import time
 from typing import Callable, Sequence
 
 import numpy as np
@@ -42,7 +43,7 @@ __all__ = [
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
-    "batch_intersect", "batch_count", "batch_autotune",
+    "batch_intersect", "batch_count", "batch_autotune", "Server",
 ]
 
 
@@ -323,6 +324,95 @@ def batch_autotune(pool, a_off, a_len, b_off, b_len, *, reps: int = 3,
     v, r = C.c_int(), C.c_uint32()
     ctx.check(lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v), C.byref(r)))
     return int(v.value), int(r.value)
+
+
+# ---------------------------------------------------------------------------
+# serving k-set queries against a resident index
+
+class Server:
+    """A query server over a posting-list index (setops_srv_*): queries of
+    k list ids, answered by their ascending intersection, batched on the GPU
+    as they arrive."""
+
+    def __init__(self, pool, offs, lens, *, budget: int = 0, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._pool = np.ascontiguousarray(pool, dtype=np.uint32)
+        self._offs = np.ascontiguousarray(offs, dtype=np.uint64)
+        self._lens = np.ascontiguousarray(lens, dtype=np.uint64)
+        h = C.c_void_p()
+        self.ctx.check(lib.setops_srv_start(
+            self.ctx.handle, self._pool.ctypes.data, self._pool.size, self._offs.ctypes.data,
+            self._lens.ctypes.data, self._lens.size, budget, HOST, C.byref(h)))
+        self._h = h
+        self._buf = np.empty(1 << 16, np.uint32)
+        self._early = {}  # results polled while waiting for another tag
+
+    def submit(self, list_ids, tag: int) -> None:
+        ids = np.ascontiguousarray(list_ids, dtype=np.uint32)
+        rc = lib.setops_srv_submit(self._h, ids.ctypes.data, ids.size, tag)
+        if rc != 0:
+            raise SetopsError(rc, _lib.status_string(rc))
+
+    def poll(self):
+        """(tag, answer, latency_ns) of one finished query, or None."""
+        tag, n, lat = C.c_uint64(), C.c_size_t(), C.c_uint64()
+        while True:
+            rc = lib.setops_srv_poll(self._h, C.byref(tag), self._buf.ctypes.data,
+                                     self._buf.size, C.byref(n), C.byref(lat))
+            if rc == _lib.ERR_CAPACITY:
+                self._buf = np.empty(max(int(n.value), 2 * self._buf.size), np.uint32)
+                continue
+            if rc == _lib.ERR_NOT_READY:
+                return None
+            if rc != 0:
+                raise SetopsError(rc, _lib.status_string(rc))
+            return int(tag.value), self._buf[:int(n.value)].copy(), int(lat.value)
+
+    def wait(self, tag: int):
+        """Polls until the query `tag` is done (other results are kept)."""
+        while True:
+            if tag in self._early:
+                return self._early.pop(tag)
+            r = self.poll()
+            if r is None:
+                time.sleep(0)
+                continue
+            if r[0] == tag:
+                return r
+            self._early[r[0]] = r
+
+    def stats(self) -> dict:
+        v = [C.c_uint64() for _ in range(4)]
+        self.ctx.check(lib.setops_srv_stats(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("batches", "queries", "max_batch", "launches"), (x.value for x in v)))
+
+    def run_load(self, ids, ks, rate_qps: float, seed: int = 1):
+        """Open-loop Poisson load; returns (latency_ns[nq], counts[nq], elapsed_s)."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        ks = np.ascontiguousarray(ks, dtype=np.uint32)
+        nq = ks.size
+        lat = np.zeros(nq, np.uint64)
+        cnt = np.zeros(nq, np.uint64)
+        el = C.c_double()
+        rc = lib.setops_srv_run_load(self._h, ids.ctypes.data, ks.ctypes.data, ids.shape[1], nq,
+                                     rate_qps, seed, lat.ctypes.data, cnt.ctypes.data,
+                                     C.byref(el))
+        if rc != 0:
+            raise SetopsError(rc, _lib.status_string(rc))
+        return lat, cnt, float(el.value)
+
+    def stop(self) -> None:
+        if self._h is not None:
+            rc = lib.setops_srv_stop(self._h)
+            self._h = None
+            if rc != 0:
+                raise SetopsError(rc, _lib.status_string(rc))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
 
 
 # ---------------------------------------------------------------------------

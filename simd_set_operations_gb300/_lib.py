@@ -84,6 +84,11 @@ SIGNATURES = [
     ("setops_gpu_batch_get_policy", C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
     ("setops_gpu_batch_num_variants", C.c_int, []),
     ("setops_gpu_batch_autotune", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, C.c_int, uint]),
+    ("setops_srv_start", C.c_int, [vp, vp, sz, vp, vp, sz, sz, uint, C.POINTER(vp)]),
+    ("setops_srv_submit", C.c_int, [vp, vp, sz, u64]),
+    ("setops_srv_poll", C.c_int, [vp, u64p, vp, sz, szp, u64p]),
+    ("setops_srv_stats", C.c_int, [vp, u64p, u64p, u64p, u64p]),
+    ("setops_srv_stop", C.c_int, [vp]),
     # setops_bench.h
     ("setops_gen_twoset", C.c_int, [u64, C.c_double, C.c_double, sz, sz, vp, vp]),
     ("setops_gen_kset_lens", C.c_int, [sz, C.c_double, sz, szp]),
@@ -93,6 +98,9 @@ SIGNATURES = [
                                         C.c_double, C.c_double, vp, C.c_int]),
     ("setops_gen_index_lens", C.c_int, [sz, sz, C.c_double, vp]),
     ("setops_gen_index_fill", C.c_int, [u64, sz, vp, vp, u64, vp, C.c_int]),
+    ("setops_gen_queries", C.c_int, [u64, sz, sz, C.c_uint32, C.c_uint32, C.c_double, vp, vp]),
+    ("setops_srv_run_load", C.c_int, [vp, vp, vp, sz, sz, C.c_double, u64, vp, vp,
+                                      C.POINTER(C.c_double)]),
     ("setops_gen_sorted_sample", C.c_int, [u64, sz, u64, vp]),
     ("setops_datafile_write", C.c_int, [C.c_char_p, C.POINTER(vp), vp, sz]),
     ("setops_datafile_read_header", C.c_int, [C.c_char_p, u64p, vp, sz]),

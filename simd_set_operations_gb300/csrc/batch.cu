@@ -156,6 +156,12 @@ int batch_impl(setops_ctx *ctx, const uint32_t *pool, size_t pool_len, const uin
 
 }  // namespace
 
+// The batch kernel of a shape (for callers launching on their own stream).
+const KernelInfo &batch_kernel_info(bool mat, int variant) {
+  if (variant < 0 || variant >= kNumBatch) variant = 0;
+  return kBatchU32[variant][mat ? 1 : 0];
+}
+
 extern "C" {
 
 int setops_gpu_batch_intersect(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,

@@ -27,7 +27,8 @@
 namespace setops {
 
 struct BatchArgs {
-  const uint32_t *pool;   // all sets
+  const uint32_t *pool;    // all sets (A sides)
+  const uint32_t *pool_b;  // B sides when they live elsewhere (NULL: pool)
   const uint64_t *a_off;  // per pair: offset and length of both sets
   const uint64_t *a_len;
   const uint64_t *b_off;
@@ -114,7 +115,8 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchArgs p) {
     __syncthreads();  // everyone has read the ticket before it is reused
     if (k >= p.npairs) break;
     uint64_t na = p.a_len[k], nb = p.b_len[k];
-    const uint32_t *A = p.pool + p.a_off[k], *B = p.pool + p.b_off[k];
+    const uint32_t *A = p.pool + p.a_off[k];
+    const uint32_t *B = (p.pool_b ? p.pool_b : p.pool) + p.b_off[k];
     if (na > nb) {
       const uint32_t *tp = A; A = B; B = tp;
       const uint64_t tn = na; na = nb; nb = tn;

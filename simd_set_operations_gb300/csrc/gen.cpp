@@ -276,6 +276,49 @@ int setops_gen_sorted_sample(uint64_t seed, size_t n, uint64_t max_value,
   return 0;
 }
 
+int setops_gen_queries(uint64_t seed, size_t nq, size_t nlists, uint32_t kmin,
+                       uint32_t kmax, double s, uint32_t *ids, uint32_t *ks) {
+  if ((nq && (!ids || !ks)) || kmin < 1 || kmax < kmin || kmax > 16 || nlists < kmax) return -1;
+  // inverse CDF of Zipf(s) over popularity ranks 1..nlists
+  std::vector<double> cdf(nlists);
+  double acc = 0;
+  for (size_t r = 0; r < nlists; ++r) {
+    acc += 1.0 / std::pow(double(r + 1), s);
+    cdf[r] = acc;
+  }
+  Rng rng(seed);
+  for (size_t q = 0; q < nq; ++q) {
+    const uint32_t k = kmin + rng.below(uint64_t(kmax - kmin + 1));
+    ks[q] = k;
+    uint32_t *row = ids + q * kmax;
+    for (uint32_t j = 0; j < kmax; ++j) row[j] = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+      uint32_t id = 0;
+      for (int attempt = 0; attempt < 64; ++attempt) {  // distinct lists per query
+        const double u = rng.unit() * acc;
+        id = uint32_t(std::lower_bound(cdf.begin(), cdf.end(), u) - cdf.begin());
+        if (id >= nlists) id = uint32_t(nlists - 1);
+        bool dup = false;
+        for (uint32_t i = 0; i < j; ++i) dup |= row[i] == id;
+        if (!dup) break;
+        id = uint32_t(-1);
+      }
+      if (id == uint32_t(-1)) {  // heavy skew: take the first unused rank
+        for (uint32_t c = 0; c < nlists; ++c) {
+          bool used = false;
+          for (uint32_t i = 0; i < j; ++i) used |= row[i] == c;
+          if (!used) {
+            id = c;
+            break;
+          }
+        }
+      }
+      row[j] = id;
+    }
+  }
+  return 0;
+}
+
 int setops_gen_index_fill(uint64_t seed, size_t nlists, const uint64_t *lens,
                           const uint64_t *offs, uint64_t doc_space,
                           uint32_t *pool, int nthreads) {

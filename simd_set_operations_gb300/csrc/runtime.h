@@ -79,6 +79,9 @@ struct setops_ctx {
   }
 };
 
+// The batch kernel of a shape (batch.cu).
+const setops::KernelInfo &batch_kernel_info(bool mat, int variant);
+
 // Runtime helpers (runtime.cu).
 int ctx_fail(setops_ctx *ctx, int status, const std::string &what);
 int ctx_cuda(setops_ctx *ctx, cudaError_t e, const char *what);

@@ -133,6 +133,18 @@ def gen_index(seed: int, nlists: int, max_len: int = 1 << 20, s: float = 1.1,
     return PostingIndex(pool, offs, lens, doc_space)
 
 
+def gen_queries(seed: int, nq: int, nlists: int, kmin: int = 2, kmax: int = 6,
+                s: float = 1.1) -> tuple[np.ndarray, np.ndarray]:
+    """k-set queries: k uniform in [kmin, kmax], then k distinct list ids
+    drawn Zipf(s) over popularity rank.  Returns (ids[nq, kmax], ks[nq])."""
+    ids = np.zeros((nq, kmax), np.uint32)
+    ks = np.zeros(nq, np.uint32)
+    if lib.setops_gen_queries(seed, nq, nlists, kmin, kmax, s, ids.ctypes.data,
+                              ks.ctypes.data) != 0:
+        raise ValueError("setops_gen_queries: bad arguments")
+    return ids, ks
+
+
 # ---- datafile (benchmark/src/datafile.rs) ---------------------------------
 
 class DatafileError(ValueError):

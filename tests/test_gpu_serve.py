@@ -1,0 +1,75 @@
+"""Serving k-set queries (setops_srv_*): every answer must equal svs_generic
+over the query's lists (the reference's k-set path, setops/src/intersect/
+svs.rs:50-73, with naive_merge), and be the same whether the query runs alone
+or batched with others, under an open-loop Poisson load included."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import simd_set_operations_gb300 as so  # noqa: E402
+from simd_set_operations_gb300 import datasets as ds  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def index():
+    return ds.gen_index(20240612, 20000, 1 << 14, 1.1, 1 << 22)
+
+
+@pytest.fixture(scope="module")
+def queries(index):
+    return ds.gen_queries(20240613, 400, len(index), 2, 6, 1.1)
+
+
+def oracle_answers(orc, index, ids, ks):
+    groups = [[index.list(int(i)) for i in ids[q][:ks[q]]] for q in range(ks.size)]
+    outs = [np.empty(max(min(g.size for g in grp), 1), np.uint32) for grp in groups]
+    counts = orc.run_svs_groups(groups, 8, outs=outs)
+    return [o[:int(c)] for o, c in zip(outs, counts)]
+
+
+def test_serve_alone_mix_and_oracle(ctx, orc, index, queries):
+    ids, ks = queries
+    want = oracle_answers(orc, index, ids, ks)
+    with so.Server(index.pool, index.offs, index.lens, ctx=ctx) as srv:
+        # alone: one query on the GPU at a time
+        alone = []
+        for q in range(ks.size):
+            srv.submit(ids[q][:ks[q]], q)
+            tag, res, lat = srv.wait(q)
+            assert tag == q and lat > 0
+            alone.append(res)
+        # in the mix: all submitted at once, batched together
+        for q in range(ks.size):
+            srv.submit(ids[q][:ks[q]], 10_000 + q)
+        mix = {}
+        while len(mix) < ks.size:
+            r = srv.poll()
+            if r is not None:
+                mix[r[0] - 10_000] = r[1]
+        st = srv.stats()
+        assert st["max_batch"] > 1, st  # the mix really was batched
+        for q in range(ks.size):
+            assert np.array_equal(alone[q], want[q]), q
+            assert np.array_equal(mix[q], want[q]), q
+
+
+def test_serve_poisson_load(ctx, orc, index, queries):
+    ids, ks = queries
+    want = oracle_answers(orc, index, ids, ks)
+    reps = 5
+    ids_r, ks_r = np.tile(ids, (reps, 1)), np.tile(ks, reps)
+    with so.Server(index.pool, index.offs, index.lens, budget=16 << 20, ctx=ctx) as srv:
+        lat, cnt, el = srv.run_load(ids_r, ks_r, rate_qps=20000, seed=3)
+    assert el > 0 and np.all(lat > 0)
+    assert [int(c) for c in cnt] == [w.size for w in want] * reps
+
+
+def test_serve_rejects_bad_queries(ctx, index):
+    with so.Server(index.pool, index.offs, index.lens, ctx=ctx) as srv:
+        with pytest.raises(so.SetopsError):
+            srv.submit([1], 0)  # k < 2
+        with pytest.raises(so.SetopsError):
+            srv.submit([0, len(index)], 0)  # no such list
