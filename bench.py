@@ -20,6 +20,9 @@ policy picks for its size ratio.
 * ``cpu_baseline``: the reference's CPU path (oracle port: best of
   shuffling / SIMD galloping / bmiss per pair) on this host's cores.
 
+* ``serve``: the serving configuration -- k-set queries against a resident
+  index of 1M posting lists, Poisson arrivals at several rates, queries/s
+  with p50/p99 latency, beside one k-set call per query.
 * ``batch``: the batched configuration -- 100,000 uneven pairs in one
   persistent launch (policy autotuned on a sample) against one launch per
   pair on a sample of the same pairs; results checked equal.
@@ -68,6 +71,10 @@ def parse():
     p.add_argument("--no-batch", action="store_true",
                    help="skip the batched-pairs leg (100k uneven pairs in one launch)")
     p.add_argument("--batch-pairs", type=int, default=100000)
+    p.add_argument("--no-serve", action="store_true",
+                   help="skip the serving leg (k-set queries against a resident index)")
+    p.add_argument("--serve-rates", default="10000,50000,200000,1000000",
+                   help="Poisson arrival rates (queries/s) of the serving leg")
     p.add_argument("--pairs", default="0,1,2,3",
                    help="which sweep pairs to run (profiling subsets; default all)")
     return p.parse_args()
@@ -406,6 +413,75 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
     }
 
 
+SERVE_SEED = 20240612
+
+
+def serve_leg(ctx, rates) -> dict:
+    """Served k-set queries (the reference's serving configuration): a
+    resident index of 1,000,000 posting lists with rank-size Zipf(1.1)
+    lengths clipped to [1, 2^20] over 2^26 documents; queries of k ~ U{2..6}
+    lists drawn Zipf(1.1) over popularity, arriving as a Poisson stream at
+    each rate (open loop: latency from scheduled arrival to completion).
+    Beside it, the plain path: one setops_gpu_svs call per query."""
+    import ctypes as C
+
+    import torch
+
+    import simd_set_operations_gb300 as so
+    from simd_set_operations_gb300 import _lib, datasets as ds
+    L = _lib.lib
+    nl = 1_000_000
+    idx = ds.gen_index(SERVE_SEED, nl, 1 << 20, 1.1, 1 << 26)
+    nq_max = max(min(int(max(rates) * 1.0), 300_000), 20_000)
+    ids, ks = ds.gen_queries(SERVE_SEED + 1, nq_max, nl, 2, 6, 1.1)
+    out = {"workload": "1,000,000 posting lists, rank-size Zipf(1.1) lengths in [1, 2^20] "
+                       f"({int(idx.pool.size)} postings, {4 * int(idx.pool.size) / 1e6:.1f} MB "
+                       "resident) over 2^26 documents; queries k ~ U{2..6} lists, Zipf(1.1) "
+                       "over popularity; Poisson arrivals; answers materialised",
+           "rates": []}
+    with so.Server(idx.pool, idx.offs, idx.lens, budget=512 << 20, ctx=ctx) as srv:
+        srv.run_load(ids[:2000], ks[:2000], rate_qps=20000, seed=7)  # warm-up
+        for rate in rates:
+            nq = min(nq_max, max(int(rate * 1.0), 10_000))  # about a second of arrivals
+            st0 = srv.stats()
+            lat, cnt, el = srv.run_load(ids[:nq], ks[:nq], rate_qps=float(rate), seed=11)
+            st1 = srv.stats()
+            lat_ms = lat.astype(np.float64) * 1e-6
+            out["rates"].append({
+                "offered_qps": rate, "queries": nq, "achieved_qps": nq / el,
+                "p50_ms": float(np.percentile(lat_ms, 50)),
+                "p99_ms": float(np.percentile(lat_ms, 99)),
+                "mean_answer": float(cnt.mean()),
+                "batches": st1["batches"] - st0["batches"],
+                "mean_batch": (st1["queries"] - st0["queries"]) / max(st1["batches"] - st0["batches"], 1),
+            })
+    # the plain path: one synchronous k-set call per query on device pointers
+    pool = torch.from_numpy(idx.pool.view(np.int32)).cuda()
+    base = pool.data_ptr()
+    dout = torch.empty(1 << 20, dtype=torch.int32, device="cuda")
+    n = C.c_size_t()
+    times = []
+    nplain = 500
+    for q in range(nplain + 20):
+        k = int(ks[q])
+        sets = (C.c_void_p * k)(*[base + 4 * int(idx.offs[i]) for i in ids[q][:k]])
+        lens = (C.c_size_t * k)(*[int(idx.lens[i]) for i in ids[q][:k]])
+        t0 = time.perf_counter()
+        ctx.check(L.setops_gpu_svs(ctx.handle, sets, lens, k, dout.data_ptr(), dout.numel(),
+                                   C.byref(n), 0))
+        if q >= 20:
+            times.append(time.perf_counter() - t0)
+    tt = np.array(times) * 1e3
+    out["plain_one_call_per_query"] = {
+        "api": "setops_gpu_svs per query, device pointers, sequential", "queries": nplain,
+        "qps": nplain / (tt.sum() * 1e-3), "p50_ms": float(np.percentile(tt, 50)),
+        "p99_ms": float(np.percentile(tt, 99))}
+    best = max(r["achieved_qps"] for r in out["rates"])
+    out["best_served_qps"] = best
+    out["speedup_vs_plain"] = best / out["plain_one_call_per_query"]["qps"]
+    return out
+
+
 def run_gb300(args):
     import ctypes as C
 
@@ -591,6 +667,9 @@ def run_gb300(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_leg(ctx, stream, args.batch_pairs)
+    serve = None
+    if rank == 0 and not args.no_serve:
+        serve = serve_leg(ctx, [int(x) for x in args.serve_rates.split(",")])
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -600,6 +679,7 @@ def run_gb300(args):
         "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "batch": batch,
+        "serve": serve,
         "timing": {"bracket_ms_total": wall_ms, "kernel_ms_total": dev_ms,
                    "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
                            "sync inside); kernel_ms_total sums the per-launch events"},
