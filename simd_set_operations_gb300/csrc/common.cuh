@@ -62,6 +62,18 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
       : "memory");
 }
 
+// Plain arrival (no bytes expected): completes a phase whose copy is empty.
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses (and
+// those it has synchronised with) before later async-proxy ones: used before
+// a bulk copy overwrites a buffer that threads have been reading.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(

@@ -5,6 +5,7 @@
 #include "gallop.cuh"
 #include "merge.cuh"
 #include "tile.cuh"
+#include "window.cuh"
 
 namespace setops {
 
@@ -23,6 +24,13 @@ KernelInfo mk_gallop(const char *name) {
   return KernelInfo{reinterpret_cast<const void *>(
                         &gallop_kernel<NT, GS, ITEMS, NSAMP, BSR, MAT>),
                     NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name};
+}
+
+template <int NT, int UA, int UB, int VW, int MINB, bool MAT>
+KernelInfo mk_window(const char *name) {
+  using Cfg = WindowCfg<NT, UA, UB, VW, MAT>;
+  return KernelInfo{reinterpret_cast<const void *>(&window_kernel<NT, UA, UB, VW, MINB, MAT>), NT,
+                    Cfg::kSmemBytes, Cfg::kTile, name, MAT};
 }
 
 template <int NT, int TA, int VW, int MINB, bool MAT>
@@ -57,16 +65,22 @@ const KernelInfo kMergeBsr[][2] = {
     MERGE_ROW(8, 2048, 2, 2, 4096, true),  // 1: 96 KB
     MERGE_ROW(8, 1024, 2, 2, 4096, true),  // 2: 64 KB
 };
-// NT threads; A tiles of TA elements; T of VW words (dense tiles span
-// < 32*VW values); MINB CTAs per SM the register budget allows
+// Window kernels: NT threads; UA / UB 16-byte loads per thread for an A tile
+// (4*UA*NT elements) / a B window (4*UB*NT); T of VW words (dense tiles span
+// < 32*VW values); MINB CTAs per SM.  Tile kernel: A tiles of TA elements,
+// B ranges searched per tile.
+#define WINDOW_ROW(NT, UA, UB, VW, MINB)                                                     \
+  {mk_window<NT, UA, UB, VW, MINB, false>("window_" #NT "_a" #UA "_b" #UB "_t" #VW "_m" #MINB), \
+   mk_window<NT, UA, UB, VW, MINB, true>("window_" #NT "_a" #UA "_b" #UB "_t" #VW "_m" #MINB)}
 #define TILE_ROW(NT, TA, VW, MINB)                                             \
   {mk_tile<NT, TA, VW, MINB, false>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB), \
    mk_tile<NT, TA, VW, MINB, true>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB)}
 const KernelInfo kBitmapU32[][2] = {
-    TILE_ROW(256, 4096, 4096, 8),  // 0: 16 / 32 KB shared; 8 CTAs/SM (count), 7 (mat.)
-    TILE_ROW(256, 4096, 4096, 6),  // 1: 6 CTAs/SM
-    TILE_ROW(256, 2048, 2048, 8),  // 2: smaller tiles
-    TILE_ROW(256, 4096, 4096, 4),  // 3: more registers per thread
+    WINDOW_ROW(128, 4, 5, 2048, 8),  // 0: 2048-element tiles, 8-9 CTAs/SM
+    WINDOW_ROW(256, 4, 6, 4096, 4),  // 1: 4096-element tiles, 4 CTAs/SM
+    WINDOW_ROW(256, 4, 5, 4096, 5),  // 2: 5 CTAs/SM
+    WINDOW_ROW(256, 4, 4, 4096, 6),  // 3: 6 CTAs/SM
+    TILE_ROW(256, 4096, 4096, 8),    // 4: tile kernel (a B search per tile)
 };
 
 // GS lanes per element (1 = thread per element with IT interleaved

@@ -1,0 +1,437 @@
+// window.cuh -- tiled bitmap intersection of two large sorted, duplicate-free
+// u32 arrays with B read in speculative windows.  Same result as naive_merge
+// (setops/src/intersect/merge.rs:7-33) with the Counter or writer visitors
+// (setops/src/visitor.rs:24-49, 759-950): the same elements, ascending.
+//
+// Work layout
+// -----------
+// A is the smaller input.  CTA c of the G resident CTAs owns the run
+// A[c*na/G, (c+1)*na/G); its first B index b0 (the first B value >= the run's
+// first value) is found once, by one warp, while the other warps load the
+// first A tile.  Then, tile by tile (TA = 4*UA*NT elements of A, values
+// [w, alast]):
+//
+//   1. every thread loads UA 16-byte words of the tile (all loads in flight
+//      at once) and sets their bits in bitmap T of the value range (dense:
+//      alast - w < 32*VW), or keeps them as a sorted table in shared memory
+//      (sparse);
+//   2. B is read from the current position b in windows of 4*UB*NT elements
+//      (UB 16-byte loads per thread in flight): each element tests its bit in
+//      T (an element below w or above alast lands on a zero bit: the index is
+//      clamped onto a zero word) or binary-searches the sparse table.  The
+//      window is a guess -- the tile's B range is not searched for -- so the
+//      elements up to alast are counted: sorted, they are a prefix of the
+//      window, b moves past them, and when the whole window was used the
+//      next window follows.  An element above alast is read again by the
+//      next tile (from L2; it was just loaded);
+//   3. count mode counts; materialise mode marks matches in bitmap M (in
+//      value order) and appends the tile's matches, in order, to the CTA's
+//      staging run, which starts at the CTA's first A index (an exclusive
+//      region);
+//   4. T is cleared.
+//
+// So a tile costs two rounds of loads (A, then B) and no search, and every
+// thread keeps four 16-byte loads in flight.  Materialise mode then
+// publishes each CTA's count, passes one grid-wide barrier (cooperative
+// launch: every CTA resident) and copies the CTA's staged run to the sum of
+// its predecessors' counts.  Count mode adds per-CTA totals atomically.
+//
+// 16-byte loads need 16-byte aligned addresses: a tile's or window's at most
+// three elements before the first aligned word and after the last are read
+// with plain loads, so any 4-byte alignment works and no load reaches past
+// either array.
+#pragma once
+
+#include "tile.cuh"
+
+namespace setops {
+
+template <int NT, int UA, int UB, int VW, bool MAT>
+struct WindowCfg {
+  static_assert(NT % 32 == 0 && NT >= 64, "whole warps");
+  static_assert(UA >= 1 && UB >= 1, "loads per thread");
+  static constexpr int kTile = 4 * UA * NT;    // A elements per tile (aligned body)
+  static constexpr int kWindow = 4 * UB * NT;  // B elements per window (aligned body)
+  static_assert((VW & (VW - 1)) == 0 && VW >= kTile, "a sparse tile (+6 end elements) fits T");
+  static constexpr uint32_t kSpan = uint32_t(VW) * 32u;
+  static constexpr int kTabWords = VW + 8;
+  static constexpr int kMWords = MAT ? VW : 0;
+  static constexpr int kSWords = MAT ? VW / 32 : 0;  // summary: one bit per M word
+  static_assert(VW / 32 <= NT && (VW / 32) % 4 == 0, "one summary word per thread");
+  static constexpr size_t kSmemBytes = size_t(kTabWords + kMWords + kSWords) * 4;
+};
+
+template <int NT, int UA, int UB, int VW, int MINB, bool MAT>
+__global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
+  using Cfg = WindowCfg<NT, UA, UB, VW, MAT>;
+  constexpr int NW = NT / 32;
+  constexpr uint32_t SPAN = Cfg::kSpan;
+  constexpr uint32_t TA = Cfg::kTile;
+
+  extern __shared__ __align__(128) uint32_t smem[];
+  uint32_t *tab = smem;                    // T (dense) or the sorted A tile (sparse)
+  uint32_t *mbits = smem + Cfg::kTabWords; // M: matches of the tile (materialise)
+  uint32_t *sbits = mbits + Cfg::kMWords;  // S: M words holding a match
+  __shared__ unsigned long long s_b0;
+  __shared__ uint32_t s_le[3];  // B elements of a window up to alast (rotating)
+  __shared__ uint32_t warp_sums[NW];
+  __shared__ unsigned long long red[NW];
+
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+  // ---- problem (A = smaller set) ----
+  uint64_t na = p.na_dev ? *p.na_dev : p.na;
+  uint64_t nb = p.nb_dev ? *p.nb_dev : p.nb;
+  const uint32_t *A = p.a, *B = p.b;
+  if (na > nb) {
+    const uint32_t *tp = A; A = B; B = tp;
+    const uint64_t tn = na; na = nb; nb = tn;
+  }
+  if (skip_by_rule(p.skip_rule, p.ratio_thr, na, nb)) return;
+  const uint32_t G = gridDim.x;
+  const uint64_t ca0 = nb ? uint64_t(blockIdx.x) * na / G : 0;
+  const uint64_t ca1 = nb ? (uint64_t(blockIdx.x) + 1) * na / G : 0;
+
+  for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords + Cfg::kSWords) / 4; i += NT)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+  if (t < 3) s_le[t] = 0;
+  __syncthreads();  // T zero before any thread inserts
+
+  // the run's aligned body [v0, v1): tile k covers [v0 + k*TA, v0 + (k+1)*TA)
+  // of it; the head [ca0, v0) joins tile 0 and the tail [v1, ca1) the last
+  uint64_t v0, v1;
+  aligned_body(A, ca0, ca1, v0, v1);
+  const uint32_t ntiles =
+      ca1 > ca0 ? uint32_t(v1 > v0 ? (v1 - v0 + TA - 1) / TA : 1) : 0u;
+  // 16-byte words: element i of X is in word (xmis + i) / 4 of X4
+  const uint64_t amis = (reinterpret_cast<uintptr_t>(A) >> 2) & 3;
+  const uint64_t bmis = (reinterpret_cast<uintptr_t>(B) >> 2) & 3;
+  const uint4 *A4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(A) & ~uintptr_t(15));
+  const uint4 *B4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(B) & ~uintptr_t(15));
+
+  // warp 0: b0 = first B index with a value >= A[ca0]
+  if (ntiles && warp == 0) {
+    const uint32_t key = __ldg(A + ca0);
+    const uint32_t bfirst = __ldg(B), blast = __ldg(B + nb - 1);
+    const uint64_t est =
+        (blast <= bfirst || key <= bfirst)
+            ? 0
+            : uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
+    const uint64_t r = warp_lower_bound(B, nb, key, est);
+    if (lane == 0) s_b0 = r;
+  }
+
+  uint32_t cnt = 0;     // count mode: this thread's matches
+  uint64_t staged = 0;  // materialise: matches staged so far
+  uint32_t *dst = MAT ? p.stage + ca0 : nullptr;
+  uint64_t b = 0;       // first B element not yet consumed
+  uint32_t wc = 0;      // windows so far (s_le slot)
+
+  for (uint32_t k = 0; k < ntiles; ++k) {
+    // ---- 1. the A tile ----
+    const uint64_t body0 = v0 + uint64_t(k) * TA;
+    const uint64_t body1 = (body0 + TA < v1) ? body0 + TA : v1;
+    const uint64_t e0 = (k == 0) ? ca0 : body0;  // tile [e0, e1)
+    const uint64_t e1 = (k + 1 == ntiles) ? ca1 : body1;
+    const uint32_t nt = uint32_t(e1 - e0);
+    const uint32_t w = __ldg(A + e0), alast = __ldg(A + e1 - 1);
+    const uint32_t span = alast - w;
+    const bool dense = span < SPAN;
+    {
+      const uint4 *ta = A4 + ((amis + body0) >> 2);  // the body's 16-byte words
+      const uint32_t nq = uint32_t((body1 - body0) >> 2);
+      const bool full = nq == uint32_t(UA * NT);
+      uint4 va[UA];
+      if (full) {
+#pragma unroll
+        for (int u = 0; u < UA; ++u) va[u] = __ldcs(ta + (u * NT + t));
+      } else {
+#pragma unroll
+        for (int u = 0; u < UA; ++u)
+          va[u] = uint32_t(u * NT + t) < nq ? __ldcs(ta + (u * NT + t)) : make_uint4(0, 0, 0, 0);
+      }
+      // head / tail elements (tile 0 / last tile): plain loads
+      const uint32_t nh = uint32_t(body0 - e0), ntl = uint32_t(e1 - body1);
+      const bool is_h = uint32_t(t) < nh;
+      const bool is_t = uint32_t(t) >= 32 && uint32_t(t) < 32 + ntl;
+      uint32_t xe = 0;
+      if (is_h) xe = __ldg(A + e0 + t);
+      else if (is_t) xe = __ldg(A + body1 + (t - 32));
+      if (dense) {
+        // (sorted input: every offset is at most span; the clamp keeps T's
+        // bounds)
+        auto ins = [&](uint32_t x) {
+          const uint32_t o = min(x - w, span);
+          atomicOr(&tab[o >> 5], 1u << (o & 31));
+        };
+        auto ins4 = [&](const uint4 &v) {
+          ins(v.x);
+          ins(v.y);
+          ins(v.z);
+          ins(v.w);
+        };
+        if (full) {
+#pragma unroll
+          for (int u = 0; u < UA; ++u) ins4(va[u]);
+        } else {
+#pragma unroll
+          for (int u = 0; u < UA; ++u)
+            if (uint32_t(u * NT + t) < nq) ins4(va[u]);
+        }
+        if (is_h || is_t) ins(xe);
+      } else {
+        // sparse: the tile itself in T's words, in order
+#pragma unroll
+        for (int u = 0; u < UA; ++u) {
+          const uint32_t qq = uint32_t(u * NT + t);
+          if (qq < nq) {  // (tile 0 may start up to three head elements in: 4-byte stores)
+            uint32_t *d = tab + nh + 4 * qq;
+            d[0] = va[u].x;
+            d[1] = va[u].y;
+            d[2] = va[u].z;
+            d[3] = va[u].w;
+          }
+        }
+        if (is_h) tab[t] = xe;
+        else if (is_t) tab[uint32_t(body1 - e0) + (t - 32)] = xe;
+      }
+    }
+    __syncthreads();
+    if (k == 0) b = s_b0;
+
+    // ---- 2. B windows from b ----
+    // Each element is probed; the elements up to alast are counted in whole
+    // 16-byte words (a word counts when its last element is at most alast),
+    // so b may stop up to three elements short of the first element above
+    // alast.  Those elements are below the next tile's first value: probed
+    // again, they match nothing.
+    auto mark = [&](uint32_t o) {  // a match at M bit o (rare)
+      atomicOr(&mbits[o >> 5], 1u << (o & 31));
+      atomicOr(&sbits[o >> 10], 1u << ((o >> 5) & 31));
+    };
+    auto probe_dense = [&](uint32_t x) {
+      const uint32_t o = min(x - w, span + 1);
+      const uint32_t hit = __funnelshift_r(tab[o >> 5], 0u, o) & 1u;
+      if (MAT) {
+        if (hit) mark(o);
+      } else {
+        cnt += hit;
+      }
+    };
+    // materialise, dense: four probes, then one branch for the (rare) hits
+    auto probe4_dense_mat = [&](const uint4 &v) {
+      const uint32_t o0 = min(v.x - w, span + 1), o1 = min(v.y - w, span + 1);
+      const uint32_t o2 = min(v.z - w, span + 1), o3 = min(v.w - w, span + 1);
+      const uint32_t h = (__funnelshift_r(tab[o0 >> 5], 0u, o0) & 1u) |
+                         ((__funnelshift_r(tab[o1 >> 5], 0u, o1) & 1u) << 1) |
+                         ((__funnelshift_r(tab[o2 >> 5], 0u, o2) & 1u) << 2) |
+                         ((__funnelshift_r(tab[o3 >> 5], 0u, o3) & 1u) << 3);
+      if (h) {
+        if (h & 1u) mark(o0);
+        if (h & 2u) mark(o1);
+        if (h & 4u) mark(o2);
+        if (h & 8u) mark(o3);
+      }
+    };
+    auto probe_sparse = [&](uint32_t x) {
+      uint32_t lo = 0, len = nt;
+      while (len > 0) {
+        const uint32_t hh = len >> 1;
+        if (tab[lo + hh] < x) {
+          lo += hh + 1;
+          len -= hh + 1;
+        } else {
+          len = hh;
+        }
+      }
+      if (lo < nt && tab[lo] == x) {  // M bit by A position
+        if (MAT) mark(lo);
+        else ++cnt;
+      }
+    };
+    for (;;) {
+      if (b >= nb) break;
+      // window [b, we): aligned words [qa, qe) plus plain-loaded ends
+      const uint64_t ab = b + ((4 - ((bmis + b) & 3)) & 3);  // first aligned index >= b
+      const uint64_t ha = ab < nb ? ab : nb;                 // head [b, ha)
+      const uint64_t qa = (bmis + ha) >> 2;
+      const uint64_t nbq = (bmis + nb) >> 2;                 // words wholly inside B
+      const uint64_t qe = (qa + UB * NT < nbq) ? qa + UB * NT : nbq;
+      const uint64_t bodyend = qe > qa ? (qe << 2) - bmis : ha;
+      // the tail after the last whole word belongs to the window only when
+      // the window reaches B's end
+      const uint64_t we = (qe == nbq) ? nb : bodyend;
+      const uint4 *wq = B4 + qa;
+      const uint32_t nq = uint32_t(qe - qa);
+      const bool full = nq == uint32_t(UB * NT);
+      uint32_t le = 0;  // elements up to alast: head / tail one by one, words x4
+      {
+        uint4 vb[UB];
+        if (full) {
+#pragma unroll
+          for (int u = 0; u < UB; ++u) vb[u] = __ldcs(wq + (u * NT + t));
+        } else {
+#pragma unroll
+          for (int u = 0; u < UB; ++u)
+            vb[u] = uint32_t(u * NT + t) < nq ? __ldcs(wq + (u * NT + t)) : make_uint4(0, 0, 0, 0);
+        }
+        const uint32_t nh = uint32_t(ha - b), ntl = uint32_t(we - bodyend);
+        const bool is_h = uint32_t(t) < nh;
+        const bool is_t = uint32_t(t) >= 32 && uint32_t(t) < 32 + ntl;
+        uint32_t xe = 0;
+        if (is_h) xe = __ldg(B + b + t);
+        else if (is_t) xe = __ldg(B + bodyend + (t - 32));
+        auto run = [&](auto probe, auto probe4) {
+          auto p4 = [&](const uint4 &v) {
+            probe4(v);
+            le += v.w <= alast ? 4u : 0u;
+          };
+          if (full) {
+#pragma unroll
+            for (int u = 0; u < UB; ++u) p4(vb[u]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < UB; ++u)
+              if (uint32_t(u * NT + t) < nq) p4(vb[u]);
+          }
+          if (is_h || is_t) {
+            probe(xe);
+            le += xe <= alast ? 1u : 0u;
+          }
+        };
+        auto each4 = [](auto probe) {
+          return [probe](const uint4 &v) {
+            probe(v.x);
+            probe(v.y);
+            probe(v.z);
+            probe(v.w);
+          };
+        };
+        if (dense) {
+          if (MAT) run(probe_dense, probe4_dense_mat);
+          else run(probe_dense, each4(probe_dense));
+        } else {
+          run(probe_sparse, each4(probe_sparse));
+        }
+      }
+      // one barrier per window: slot wc%3 sums this window; the slot of two
+      // windows on is cleared (its last readers passed this barrier)
+      le = __reduce_add_sync(0xffffffffu, le);
+      if (lane == 0 && le) atomicAdd(&s_le[wc % 3], le);
+      __syncthreads();
+      const uint32_t used = s_le[wc % 3];
+      if (t == 0) s_le[(wc + 2) % 3] = 0;
+      ++wc;
+      b += used;
+      if (b < we) break;  // an element above alast: the tile is done
+    }
+
+    // ---- 3. output (materialise) and clearing ----
+    const uint32_t mw = dense ? (span >> 5) + 1 : (nt + 31) / 32;  // M / T words in use
+    if (MAT) {
+      // thread t < sw owns summary word t, i.e. M words [32t, 32t + 32):
+      // counts its matches, takes its place by a block scan, writes them
+      const uint32_t sw = (mw + 31) / 32;
+      const uint32_t sv = uint32_t(t) < sw ? sbits[t] : 0u;
+      uint32_t pc = 0;
+      for (uint32_t r = sv; r; r &= r - 1) pc += __popc(mbits[32u * t + uint32_t(__ffs(r) - 1)]);
+      uint32_t incl = pc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (lane == 31) warp_sums[warp] = incl;
+      __syncthreads();
+      uint32_t before = 0, tot = 0;
+#pragma unroll
+      for (int q = 0; q < NW; ++q) {
+        const uint32_t sm = warp_sums[q];
+        before += (q < warp) ? sm : 0u;
+        tot += sm;
+      }
+      uint64_t q = staged + before + incl - pc;
+      for (uint32_t r = sv; r; r &= r - 1) {
+        const uint32_t i = 32u * t + uint32_t(__ffs(r) - 1);
+        uint32_t m = mbits[i];
+        mbits[i] = 0;
+        while (m) {
+          const uint32_t bit = i * 32u + uint32_t(__ffs(m) - 1);
+          m &= m - 1;
+          dst[q++] = dense ? w + bit : tab[bit];
+        }
+      }
+      if (sv) sbits[t] = 0;
+      staged += tot;
+      __syncthreads();  // sparse: the table was read above; warp sums reused
+    }
+    {
+      // clear T (dense: the words used; sparse: the tile)
+      const uint32_t tw = dense ? mw : nt;
+      for (uint32_t i = uint32_t(t); i < tw; i += NT) tab[i] = 0;
+    }
+    __syncthreads();  // T clear before the next tile's insertion
+  }
+
+  // ---- combine ----
+  if (!MAT) {
+    uint64_t v = cnt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (t == 0) {
+      unsigned long long sm = 0;
+      for (int q = 0; q < NW; ++q) sm += red[q];
+      if (sm) atomicAdd(&p.sync->acc, sm);
+      __threadfence();
+      const uint32_t prev = atomicAdd(&p.sync->done, 1u);
+      if (prev == G - 1) {
+        *p.out_len = atomicExch(&p.sync->acc, 0ull);
+        p.sync->ticket = 0;
+        p.sync->done = 0;
+        __threadfence();
+      }
+    }
+    return;
+  }
+
+  if constexpr (MAT) {
+    if (t == 0) p.coranks[blockIdx.x] = staged;
+    if (!grid_barrier(&p.sync->done, G, p.err)) return;
+    // counts of CTAs 0..c-1 (plain loads: every CTA published before the
+    // barrier), four independent loads per thread per step
+    uint64_t before = 0;
+    {
+      uint32_t c = uint32_t(t);
+      for (; c + 3 * NT < blockIdx.x; c += 4 * NT)
+        before += (p.coranks[c] + p.coranks[c + NT]) + (p.coranks[c + 2 * NT] + p.coranks[c + 3 * NT]);
+      for (; c < blockIdx.x; c += NT) before += p.coranks[c];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) red[warp] = before;
+    __syncthreads();
+    uint64_t ex = 0;
+#pragma unroll
+    for (int q = 0; q < NW; ++q) ex += red[q];
+    if (ex + staged > p.out_cap) {
+      if (t == 0) record_error(p.err, DEV_ERR_CAPACITY);
+    } else {
+      for (uint64_t q = uint64_t(t); q < staged; q += NT) p.out[ex + q] = p.stage[ca0 + q];
+      if (blockIdx.x == G - 1 && t == 0) *p.out_len = ex + staged;
+    }
+    if (t == 0) {
+      __threadfence();
+      const unsigned long long prev = atomicAdd(&p.sync->acc, 1ull);
+      if (prev == G - 1) {
+        p.sync->ticket = 0;
+        p.sync->done = 0;
+        p.sync->acc = 0;
+        __threadfence();
+      }
+    }
+  }
+}
+
+}  // namespace setops
