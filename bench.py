@@ -309,7 +309,7 @@ def read_peak():
 def read_traffic():
     """DRAM bytes per launch of the headline kernel from the committed ncu
     summary (profiles/), or None."""
-    f = ROOT / "profiles" / "bitmap_2e24x2e24_ncu.md"
+    f = ROOT / "profiles" / "window_2e24x2e24_ncu.md"
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read_text())
@@ -590,7 +590,7 @@ def run_gb300(args):
     traffic = read_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "tile_kernel (bitmap; 2^24 x 2^24 pair, materialise)",
+                "kernel": "window_kernel (bitmap tiles, B in windows; 2^24 x 2^24 pair, materialise)",
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "launch_ms_mean": head_ms, "peak_source": f"{peak_kind} (hbm_gbs)"}
     sweep = []
