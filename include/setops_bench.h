@@ -70,6 +70,14 @@ int setops_gen_index_fill(uint64_t seed, size_t nlists, const uint64_t *lens,
 int setops_gen_queries(uint64_t seed, size_t nq, size_t nlists, uint32_t kmin,
                        uint32_t kmax, double s, uint32_t *ids, uint32_t *ks);
 
+/* BSR encoding of many sorted sets of one pool (BsrVec::from_sorted,
+ * setops/src/bsr.rs:140-163): set i = pool[offs[i], +lens[i]) becomes
+ * wlens[i] words at bases/states[woffs[i], ...), sets packed in order.
+ * bases/states need room for sum(lens) words. */
+int setops_gen_bsr_encode(const uint32_t *pool, size_t nsets, const uint64_t *offs,
+                          const uint64_t *lens, uint32_t *bases, uint32_t *states,
+                          uint64_t *woffs, uint64_t *wlens);
+
 /* Open-loop load for a server: query q (ids row q of an nq x kstride array,
  * ks[q] ids) arrives at the q-th point of a Poisson process of rate
  * rate_qps; latency_ns[q] runs from that arrival to completion, counts[q]

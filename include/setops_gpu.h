@@ -194,6 +194,23 @@ int setops_gpu_batch_count(setops_ctx *ctx, const uint32_t *pool, size_t pool_le
 int setops_gpu_batch_set_policy(setops_ctx *ctx, int variant, uint32_t search_ratio);
 int setops_gpu_batch_get_policy(const setops_ctx *ctx, int *variant, uint32_t *search_ratio);
 int setops_gpu_batch_num_variants(void);
+/* The same batch for BSR sets (Intersect2Bsr per pair, setops/src/bsr.rs:16;
+ * result = branchless_merge_bsr, setops/src/intersect/merge.rs:62-87): every
+ * set is (bases[off, +len), states[off, +len)) of one pool, lengths and
+ * offsets in words; pair p's result words go to out_bases/out_states at
+ * out_off[p] (NULL: offsets from a device scan of min(a_len, b_len)), its
+ * word count to out_lens[p].  Capacity per pair: min(a_len, b_len) words. */
+int setops_gpu_batch_intersect_bsr(setops_ctx *ctx, const uint32_t *bases,
+                                   const uint32_t *states, size_t pool_len,
+                                   const uint64_t *a_off, const uint64_t *a_len,
+                                   const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                                   uint32_t *out_bases, uint32_t *out_states, size_t out_cap,
+                                   const uint64_t *out_off, uint64_t *out_lens, unsigned flags);
+/* Counter visitor per BSR pair (popcount sums, setops/src/visitor.rs:399-403). */
+int setops_gpu_batch_count_bsr(setops_ctx *ctx, const uint32_t *bases, const uint32_t *states,
+                               size_t pool_len, const uint64_t *a_off, const uint64_t *a_len,
+                               const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                               uint64_t *counts, unsigned flags);
 /* Autotuner: times every kernel shape with several search ratios on the
  * given sample batch (materialising, `reps` timed runs each) and keeps the
  * fastest as the batch policy.  Plays the role of the reference's per-ISA

@@ -43,7 +43,8 @@ __all__ = [
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
-    "batch_intersect", "batch_count", "batch_autotune", "Server",
+    "batch_intersect", "batch_count", "batch_intersect_bsr", "batch_count_bsr", "batch_autotune",
+    "Server",
 ]
 
 
@@ -308,6 +309,45 @@ def batch_count(pool, a_off, a_len, b_off, b_len, *, ctx: Context | None = None)
     ctx.check(lib.setops_gpu_batch_count(
         ctx.handle, pool.ctypes.data, pool.size, a_off.ctypes.data, a_len.ctypes.data,
         b_off.ctypes.data, b_len.ctypes.data, a_len.size, counts.ctypes.data, HOST))
+    return counts
+
+
+def batch_intersect_bsr(bases, states, a_off, a_len, b_off, b_len, *,
+                        ctx: Context | None = None):
+    """Intersects every BSR pair of a batch in one launch (host arrays): pair
+    p is words [a_off[p], +a_len[p]) and [b_off[p], +b_len[p]) of (bases,
+    states).  Returns (out_bases, out_states, out_off, out_lens)."""
+    ctx = ctx or default_context()
+    bases = np.ascontiguousarray(bases, dtype=np.uint32)
+    states = np.ascontiguousarray(states, dtype=np.uint32)
+    a_off, a_len, b_off, b_len = _u64(a_off), _u64(a_len), _u64(b_off), _u64(b_len)
+    n = a_len.size
+    caps = np.minimum(a_len, b_len)
+    out_off = np.zeros(n, np.uint64)
+    if n:
+        out_off[1:] = np.cumsum(caps[:-1])
+    cap = max(int(caps.sum()), 1)
+    ob, os_ = np.empty(cap, np.uint32), np.empty(cap, np.uint32)
+    lens = np.zeros(n, np.uint64)
+    ctx.check(lib.setops_gpu_batch_intersect_bsr(
+        ctx.handle, bases.ctypes.data, states.ctypes.data, bases.size, a_off.ctypes.data,
+        a_len.ctypes.data, b_off.ctypes.data, b_len.ctypes.data, n, ob.ctypes.data,
+        os_.ctypes.data, cap, out_off.ctypes.data, lens.ctypes.data, HOST))
+    return ob, os_, out_off, lens
+
+
+def batch_count_bsr(bases, states, a_off, a_len, b_off, b_len, *,
+                    ctx: Context | None = None) -> np.ndarray:
+    """Per-pair element counts (popcount sums) of a BSR batch in one launch."""
+    ctx = ctx or default_context()
+    bases = np.ascontiguousarray(bases, dtype=np.uint32)
+    states = np.ascontiguousarray(states, dtype=np.uint32)
+    a_off, a_len, b_off, b_len = _u64(a_off), _u64(a_len), _u64(b_off), _u64(b_len)
+    counts = np.zeros(a_len.size, np.uint64)
+    ctx.check(lib.setops_gpu_batch_count_bsr(
+        ctx.handle, bases.ctypes.data, states.ctypes.data, bases.size, a_off.ctypes.data,
+        a_len.ctypes.data, b_off.ctypes.data, b_len.ctypes.data, a_len.size,
+        counts.ctypes.data, HOST))
     return counts
 
 

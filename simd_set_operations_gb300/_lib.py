@@ -80,6 +80,9 @@ SIGNATURES = [
     ("setops_gpu_intersect_noalloc", C.c_int, [vp, sz, vp, sz, vp, sz, szp, vp]),
     ("setops_gpu_batch_intersect", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, sz, vp, vp, uint]),
     ("setops_gpu_batch_count", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, uint]),
+    ("setops_gpu_batch_intersect_bsr", C.c_int,
+     [vp, vp, vp, sz, vp, vp, vp, vp, sz, vp, vp, sz, vp, vp, uint]),
+    ("setops_gpu_batch_count_bsr", C.c_int, [vp, vp, vp, sz, vp, vp, vp, vp, sz, vp, uint]),
     ("setops_gpu_batch_set_policy", C.c_int, [vp, C.c_int, C.c_uint32]),
     ("setops_gpu_batch_get_policy", C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
     ("setops_gpu_batch_num_variants", C.c_int, []),
@@ -99,6 +102,7 @@ SIGNATURES = [
     ("setops_gen_index_lens", C.c_int, [sz, sz, C.c_double, vp]),
     ("setops_gen_index_fill", C.c_int, [u64, sz, vp, vp, u64, vp, C.c_int]),
     ("setops_gen_queries", C.c_int, [u64, sz, sz, C.c_uint32, C.c_uint32, C.c_double, vp, vp]),
+    ("setops_gen_bsr_encode", C.c_int, [vp, sz, vp, vp, vp, vp, vp, vp]),
     ("setops_srv_run_load", C.c_int, [vp, vp, vp, sz, sz, C.c_double, u64, vp, vp,
                                       C.POINTER(C.c_double)]),
     ("setops_gen_sorted_sample", C.c_int, [u64, sz, u64, vp]),

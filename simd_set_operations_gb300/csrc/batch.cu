@@ -154,6 +154,112 @@ int batch_impl(setops_ctx *ctx, const uint32_t *pool, size_t pool_len, const uin
   return ctx_check_device(ctx);  // waits; reports device-side errors
 }
 
+// ---- BSR pairs ----
+constexpr int kBsrThreads = 256;
+constexpr int kBsrCapWords = 2048;  // longer set staged in shared memory up to this many words
+
+int launch_batch_bsr(setops_ctx *ctx, const BatchBsrArgs &a0, bool mat) {
+  const void *fn = mat ? reinterpret_cast<const void *>(&batch_bsr_kernel<kBsrThreads, kBsrCapWords, true>)
+                       : reinterpret_cast<const void *>(&batch_bsr_kernel<kBsrThreads, kBsrCapWords, false>);
+  const KernelInfo k{fn, kBsrThreads, 0, 1, mat ? "batch_bsr_mat" : "batch_bsr_count", false};
+  int occ = 1;
+  RK(ctx_occupancy(ctx, k, &occ));
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, a0.npairs));
+  BatchBsrArgs a = a0;
+  a.sync = ctx->sync + 1;
+  a.err = ctx->derr;
+  void *args[] = {&a};
+  return ctx_launch(ctx, k, grid, args);
+}
+
+// Shared body of the BSR batch entry points.  out_bases == NULL: count mode
+// (per-pair popcount sums to out_lens).
+int batch_bsr_impl(setops_ctx *ctx, const uint32_t *bases, const uint32_t *states,
+                   size_t pool_len, const uint64_t *a_off, const uint64_t *a_len,
+                   const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                   uint32_t *out_bases, uint32_t *out_states, size_t out_cap,
+                   const uint64_t *out_off, uint64_t *out_lens, unsigned flags) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if (npairs == 0) return SETOPS_OK;
+  if (!bases || !states || !a_off || !a_len || !b_off || !b_len || !out_lens)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL batch array");
+  const bool host = (flags & SETOPS_HOST) != 0;
+  const bool mat = out_bases != nullptr;
+  if (mat && !out_states) return ctx_fail(ctx, SETOPS_ERR_INVALID, "out_states is NULL");
+  CK(cudaSetDevice(ctx->device));
+  BatchBsrArgs a{};
+  a.bases = bases;
+  a.states = states;
+  a.a_off = a_off;
+  a.a_len = a_len;
+  a.b_off = b_off;
+  a.b_len = b_len;
+  a.npairs = npairs;
+  a.out_off = out_off;
+  a.out_bases = out_bases;
+  a.out_states = out_states;
+  a.out_lens = out_lens;
+  uint64_t need = 0;
+  if (host) {
+    RK(stage(ctx, ctx->in[0], bases, pool_len, &a.bases));
+    RK(stage(ctx, ctx->stage1, states, pool_len, &a.states));
+    RK(stage(ctx, ctx->in[1], a_off, npairs, &a.a_off));
+    RK(stage(ctx, ctx->in[2], a_len, npairs, &a.a_len));
+    RK(stage(ctx, ctx->in[3], b_off, npairs, &a.b_off));
+    RK(stage(ctx, ctx->in[4], b_len, npairs, &a.b_len));
+    for (size_t q = 0; q < npairs; ++q) {
+      if (a_off[q] + a_len[q] > pool_len || b_off[q] + b_len[q] > pool_len)
+        return ctx_fail(ctx, SETOPS_ERR_INVALID, "pair " + std::to_string(q) + " outside the pool");
+    }
+    std::vector<uint64_t> offs;
+    if (mat) {
+      const uint64_t *ho = out_off;
+      if (!ho) {
+        offs.resize(npairs);
+        for (size_t q = 0; q < npairs; ++q) {
+          offs[q] = need;
+          need += std::min(a_len[q], b_len[q]);
+        }
+        ho = offs.data();
+      } else {
+        for (size_t q = 0; q < npairs; ++q)
+          need = std::max<uint64_t>(need, out_off[q] + std::min(a_len[q], b_len[q]));
+      }
+      if (need > out_cap)
+        return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap " + std::to_string(out_cap) +
+                                                      " < " + std::to_string(need) + " output words");
+      RK(stage(ctx, ctx->in[5], ho, npairs, &a.out_off));
+      RK(buf_reserve(ctx, ctx->out0, std::max<uint64_t>(need, 1) * 4));
+      RK(buf_reserve(ctx, ctx->stage0, std::max<uint64_t>(need, 1) * 4));
+      a.out_bases = static_cast<uint32_t *>(ctx->out0.p);
+      a.out_states = static_cast<uint32_t *>(ctx->stage0.p);
+    }
+    RK(buf_reserve(ctx, ctx->out1, npairs * 8));
+    a.out_lens = static_cast<uint64_t *>(ctx->out1.p);
+    CK(cudaStreamSynchronize(ctx->st));  // `offs` is a local
+  } else if (mat && !out_off) {
+    RK(buf_reserve(ctx, ctx->in[5], npairs * 8));
+    uint64_t *o = static_cast<uint64_t *>(ctx->in[5].p);
+    batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(a_len, b_len, npairs, o, &ctx->dlen[1]);
+    CK(cudaGetLastError());
+    ++ctx->launches;
+    RK(ctx_read_u64(ctx, &ctx->dlen[1], &need));
+    if (need > out_cap)
+      return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap " + std::to_string(out_cap) +
+                                                    " < " + std::to_string(need) + " output words");
+    a.out_off = o;
+  }
+  RK(launch_batch_bsr(ctx, a, mat));
+  if (host) {
+    if (mat && need) {
+      CK(cudaMemcpyAsync(out_bases, a.out_bases, need * 4, cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(out_states, a.out_states, need * 4, cudaMemcpyDeviceToHost, ctx->st));
+    }
+    CK(cudaMemcpyAsync(out_lens, a.out_lens, npairs * 8, cudaMemcpyDeviceToHost, ctx->st));
+  }
+  return ctx_check_device(ctx);  // waits; reports device-side errors
+}
+
 }  // namespace
 
 // The batch kernel of a shape (for callers launching on their own stream).
@@ -180,6 +286,25 @@ int setops_gpu_batch_count(setops_ctx *ctx, const uint32_t *pool, size_t pool_le
                            unsigned flags) {
   return batch_impl(ctx, pool, pool_len, a_off, a_len, b_off, b_len, npairs, nullptr, 0,
                     nullptr, counts, flags);
+}
+
+int setops_gpu_batch_intersect_bsr(setops_ctx *ctx, const uint32_t *bases,
+                                   const uint32_t *states, size_t pool_len,
+                                   const uint64_t *a_off, const uint64_t *a_len,
+                                   const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                                   uint32_t *out_bases, uint32_t *out_states, size_t out_cap,
+                                   const uint64_t *out_off, uint64_t *out_lens, unsigned flags) {
+  if ((!out_bases || !out_states) && npairs) return ctx_fail(ctx, SETOPS_ERR_INVALID, "output is NULL");
+  return batch_bsr_impl(ctx, bases, states, pool_len, a_off, a_len, b_off, b_len, npairs,
+                        out_bases, out_states, out_cap, out_off, out_lens, flags);
+}
+
+int setops_gpu_batch_count_bsr(setops_ctx *ctx, const uint32_t *bases, const uint32_t *states,
+                               size_t pool_len, const uint64_t *a_off, const uint64_t *a_len,
+                               const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                               uint64_t *counts, unsigned flags) {
+  return batch_bsr_impl(ctx, bases, states, pool_len, a_off, a_len, b_off, b_len, npairs,
+                        nullptr, nullptr, 0, nullptr, counts, flags);
 }
 
 int setops_gpu_batch_set_policy(setops_ctx *ctx, int variant, uint32_t search_ratio) {

@@ -156,6 +156,132 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchArgs p) {
   }
 }
 
+// ---- BSR pairs ---------------------------------------------------------------
+// The same batch for sets in the reference's BSR form (BsrVec,
+// setops/src/bsr.rs:20-30): word i of a set is (bases[i], states[i]), bases
+// strictly increasing, states non-zero.  Pair p's result is what
+// branchless_merge_bsr (setops/src/intersect/merge.rs:62-87) emits: for every
+// base in both sets, (base, state_a & state_b) when non-zero, in base order.
+// Count mode gives the Counter visitor's popcount sum
+// (setops/src/visitor.rs:399-403).
+struct BatchBsrArgs {
+  const uint32_t *bases;   // all sets: bases and states, same offsets
+  const uint32_t *states;
+  const uint64_t *a_off, *a_len, *b_off, *b_len;  // per pair, in words
+  uint64_t npairs;
+  const uint64_t *out_off;  // per pair: output word offset (materialise)
+  uint32_t *out_bases, *out_states;
+  uint64_t *out_lens;       // per pair: result words (materialise) or popcount sum (count)
+  LaunchSync *sync;
+  int *err;
+};
+
+// Persistent CTAs pull pairs from a ticket.  Per pair (A = the set with fewer
+// words) the longer set is staged in shared memory when it fits CAPW words;
+// one thread per A word binary-searches its base there (or in global memory),
+// ANDs the states, and the non-zero words are compacted in A order (a warp
+// ballot and per-warp sums), which is base order.
+template <int NT, int CAPW, bool MAT>
+__global__ void __launch_bounds__(NT) batch_bsr_kernel(const BatchBsrArgs p) {
+  constexpr int NW = NT / 32;
+  __shared__ uint32_t sb[CAPW], ss[CAPW];
+  __shared__ uint32_t warp_sums[NW];
+  __shared__ unsigned long long red[NW];
+  __shared__ uint32_t s_pair;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (;;) {
+    if (t == 0) s_pair = atomicAdd(&p.sync->ticket, 1u);
+    __syncthreads();
+    const uint64_t k = s_pair;
+    __syncthreads();  // everyone has read the ticket before it is reused
+    if (k >= p.npairs) break;
+    uint64_t na = p.a_len[k], nb = p.b_len[k];
+    uint64_t ao = p.a_off[k], bo = p.b_off[k];
+    if (na > nb) {
+      const uint64_t tn = na; na = nb; nb = tn;
+      const uint64_t to = ao; ao = bo; bo = to;
+    }
+    const uint32_t *Ab = p.bases + ao, *As = p.states + ao;
+    const uint32_t *Bb = p.bases + bo, *Bs = p.states + bo;
+    const bool staged = nb <= uint64_t(CAPW);
+    if (staged) {
+      for (uint32_t i = uint32_t(t); i < uint32_t(nb); i += NT) {
+        sb[i] = __ldg(Bb + i);
+        ss[i] = __ldg(Bs + i);
+      }
+    }
+    __syncthreads();
+    uint64_t written = 0;  // materialise: words written for this pair
+    uint64_t pc = 0;       // count: this thread's popcount sum
+    for (uint64_t c0 = 0; c0 < na; c0 += NT) {
+      const uint64_t i = c0 + uint64_t(t);
+      uint32_t base = 0, st = 0;
+      if (i < na) {
+        base = __ldg(Ab + i);
+        uint64_t lo = 0, len = nb;
+        if (staged) {
+          while (len > 0) {
+            const uint64_t h = len >> 1;
+            if (sb[lo + h] < base) { lo += h + 1; len -= h + 1; } else { len = h; }
+          }
+          if (lo < nb && sb[lo] == base) st = __ldg(As + i) & ss[lo];
+        } else {
+          while (len > 0) {
+            const uint64_t h = len >> 1;
+            if (__ldg(Bb + lo + h) < base) { lo += h + 1; len -= h + 1; } else { len = h; }
+          }
+          if (lo < nb && __ldg(Bb + lo) == base) st = __ldg(As + i) & __ldg(Bs + lo);
+        }
+      }
+      if (!MAT) {
+        pc += uint64_t(__popc(st));
+        continue;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, st != 0);
+      if (lane == 0) warp_sums[warp] = uint32_t(__popc(m));
+      __syncthreads();
+      uint32_t before = 0, tot = 0;
+#pragma unroll
+      for (int q = 0; q < NW; ++q) {
+        const uint32_t sm = warp_sums[q];
+        before += (q < warp) ? sm : 0u;
+        tot += sm;
+      }
+      if (st) {
+        const uint64_t o = p.out_off[k] + written + before + uint32_t(__popc(m & ((1u << lane) - 1u)));
+        p.out_bases[o] = base;
+        p.out_states[o] = st;
+      }
+      written += tot;
+      __syncthreads();  // warp sums reused
+    }
+    if (!MAT) {
+      uint64_t v = pc;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp] = v;
+      __syncthreads();
+      if (t == 0) {
+        uint64_t sm = 0;
+        for (int q = 0; q < NW; ++q) sm += red[q];
+        p.out_lens[k] = sm;
+      }
+    } else if (t == 0) {
+      p.out_lens[k] = written;
+    }
+    __syncthreads();  // staged B and red reused by the next pair
+  }
+  if (t == 0) {
+    __threadfence();
+    const uint32_t prev = atomicAdd(&p.sync->done, 1u);
+    if (prev == gridDim.x - 1) {
+      p.sync->ticket = 0;
+      p.sync->done = 0;
+      __threadfence();
+    }
+  }
+}
+
 // out_off[p] = sum of min(a_len, b_len) over pairs before p (one CTA).
 template <int NT>
 __global__ void __launch_bounds__(NT) batch_offsets_kernel(const uint64_t *a_len,

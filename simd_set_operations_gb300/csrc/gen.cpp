@@ -276,6 +276,34 @@ int setops_gen_sorted_sample(uint64_t seed, size_t n, uint64_t max_value,
   return 0;
 }
 
+int setops_gen_bsr_encode(const uint32_t *pool, size_t nsets, const uint64_t *offs,
+                          const uint64_t *lens, uint32_t *bases, uint32_t *states,
+                          uint64_t *woffs, uint64_t *wlens) {
+  // BsrVec::from_sorted (setops/src/bsr.rs:140-163): one word per distinct
+  // x >> 5, its state the OR of 1 << (x & 31); sets packed back to back
+  if ((nsets && (!pool || !offs || !lens || !bases || !states || !woffs || !wlens))) return -1;
+  uint64_t w = 0;
+  for (size_t i = 0; i < nsets; ++i) {
+    const uint32_t *x = pool + offs[i];
+    const uint64_t n = lens[i];
+    woffs[i] = w;
+    uint64_t k = 0;
+    for (uint64_t j = 0; j < n; ++j) {
+      const uint32_t b = x[j] >> 5, bit = 1u << (x[j] & 31);
+      if (k > 0 && bases[w + k - 1] == b) {
+        states[w + k - 1] |= bit;
+      } else {
+        bases[w + k] = b;
+        states[w + k] = bit;
+        ++k;
+      }
+    }
+    wlens[i] = k;
+    w += k;
+  }
+  return 0;
+}
+
 int setops_gen_queries(uint64_t seed, size_t nq, size_t nlists, uint32_t kmin,
                        uint32_t kmax, double s, uint32_t *ids, uint32_t *ks) {
   if ((nq && (!ids || !ks)) || kmin < 1 || kmax < kmin || kmax > 16 || nlists < kmax) return -1;

@@ -103,6 +103,49 @@ def gen_batch(seed: int, npairs: int, min_len: int = 16, max_len: int = 1 << 16,
 
 
 @dataclass
+class BsrBatch:
+    """Pairs of BSR sets in one pool: set words are (bases[i], states[i]);
+    pair p is words [a_off[p], +a_len[p]) and [b_off[p], +b_len[p])."""
+    bases: np.ndarray
+    states: np.ndarray
+    a_off: np.ndarray
+    a_len: np.ndarray
+    b_off: np.ndarray
+    b_len: np.ndarray
+
+    def __len__(self) -> int:
+        return int(self.a_len.size)
+
+    def pair(self, p: int):
+        a0, na, b0, nb = (int(self.a_off[p]), int(self.a_len[p]), int(self.b_off[p]),
+                          int(self.b_len[p]))
+        return (self.bases[a0:a0 + na], self.states[a0:a0 + na],
+                self.bases[b0:b0 + nb], self.states[b0:b0 + nb])
+
+
+def bsr_encode_batch(batch: PairBatch) -> BsrBatch:
+    """BSR form (BsrVec::from_sorted, setops/src/bsr.rs:140-163) of every set
+    of a PairBatch, packed in one pool."""
+    n = len(batch)
+    offs = np.empty(2 * n, np.uint64)
+    lens = np.empty(2 * n, np.uint64)
+    offs[0::2], offs[1::2] = batch.a_off, batch.b_off
+    lens[0::2], lens[1::2] = batch.a_len, batch.b_len
+    cap = max(int(lens.sum()), 1)
+    bases = np.empty(cap, np.uint32)
+    states = np.empty(cap, np.uint32)
+    woffs = np.empty(2 * n, np.uint64)
+    wlens = np.empty(2 * n, np.uint64)
+    if lib.setops_gen_bsr_encode(batch.pool.ctypes.data, 2 * n, offs.ctypes.data,
+                                 lens.ctypes.data, bases.ctypes.data, states.ctypes.data,
+                                 woffs.ctypes.data, wlens.ctypes.data) != 0:
+        raise ValueError("setops_gen_bsr_encode: bad arguments")
+    total = int(wlens.sum())
+    return BsrBatch(bases[:max(total, 1)], states[:max(total, 1)], woffs[0::2].copy(),
+                    wlens[0::2].copy(), woffs[1::2].copy(), wlens[1::2].copy())
+
+
+@dataclass
 class PostingIndex:
     """Posting lists stored in one pool: list i is pool[offs[i]:offs[i]+lens[i]]."""
     pool: np.ndarray

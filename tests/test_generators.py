@@ -100,3 +100,26 @@ def test_datafile_errors(tmp_path):
     assert e.value.code == -5
     with pytest.raises(ds.DatafileError):
         ds.datafile_read(tmp_path / "missing.dat")
+
+
+def test_bsr_encode_batch_matches_oracle(orc):
+    """The bench's host BSR encoder equals BsrVec::from_sorted
+    (setops/src/bsr.rs:140-163) as the oracle restates it, set by set."""
+    b = ds.gen_batch(5, 200, 1, 1 << 12, density=(0.5, 0.5))
+    e = ds.bsr_encode_batch(b)
+    assert len(e) == len(b)
+    for p in range(len(b)):
+        a, bb = b.pair(p)
+        ba, sa, bb_, sb = e.pair(p)
+        for (wb, ws), x in (((ba, sa), a), ((bb_, sb), bb)):
+            ob, os_ = orc.bsr_from_sorted(x)
+            assert np.array_equal(wb, ob) and np.array_equal(ws, os_), p
+    # empty and one-element sets
+    pool = np.array([7, 0, 31, 32, 0xFFFFFFFF], np.uint32)
+    u = lambda x: np.array(x, np.uint64)  # noqa: E731
+    e = ds.bsr_encode_batch(ds.PairBatch(pool, u([0, 1]), u([0, 1]), u([1, 2]), u([4, 3])))
+    # pair 0: {} and {0, 31, 32, 2^32-1}; pair 1: {0} and {31, 32, 2^32-1}
+    assert [int(x) for x in e.a_len] == [0, 1] and [int(x) for x in e.b_len] == [3, 3]
+    ba, sa, bb, sb = e.pair(1)
+    assert list(ba) == [0] and list(sa) == [1]
+    assert list(bb) == [0, 1, 0x7FFFFFF] and list(sb) == [0x80000000, 1, 0x80000000]

@@ -131,3 +131,75 @@ def test_batch_autotune_keeps_results_exact(ctx, orc, generated):
         check_batch(ctx, orc, generated, want)
     finally:
         ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))
+
+
+# ---- BSR pairs ---------------------------------------------------------------
+
+def expected_bsr(orc, bb):
+    want = []
+    for p in range(len(bb)):
+        ba, sa, bb_, sb = bb.pair(p)
+        want.append(orc.branchless_merge_bsr(ba, sa, bb_, sb))
+    return want
+
+
+def check_bsr_batch(ctx, orc, bb):
+    """Every pair of a BSR batch equals branchless_merge_bsr of that pair
+    (setops/src/intersect/merge.rs:62-87), materialised and counted."""
+    want = expected_bsr(orc, bb)
+    ob, os_, off, lens = so.batch_intersect_bsr(bb.bases, bb.states, bb.a_off, bb.a_len,
+                                                bb.b_off, bb.b_len, ctx=ctx)
+    for p, (wb, ws) in enumerate(want):
+        lo, n = int(off[p]), int(lens[p])
+        assert n == wb.size, (p, n, wb.size)
+        assert np.array_equal(ob[lo:lo + n], wb) and np.array_equal(os_[lo:lo + n], ws), p
+    counts = so.batch_count_bsr(bb.bases, bb.states, bb.a_off, bb.a_len, bb.b_off, bb.b_len,
+                                ctx=ctx)
+    assert [int(c) for c in counts] == [int(np.unpackbits(ws.view(np.uint8)).sum())
+                                        for _, ws in want]
+
+
+def test_batch_bsr_dense_subset(ctx, orc):
+    # the reference's BSR subset shape (density 0.5), scaled down; sets up to
+    # 2^16 elements, so some longer sets exceed the shared-memory stage
+    b = ds.gen_batch(20240614, 400, 16, 1 << 16, density=(0.5, 0.5))
+    check_bsr_batch(ctx, orc, ds.bsr_encode_batch(b))
+
+
+def test_batch_bsr_mixed_density_and_edges(ctx, orc):
+    # edge cases (empty sides, identical, disjoint, values near 2^32, long
+    # and skewed pairs), then mixed densities
+    check_bsr_batch(ctx, orc, ds.bsr_encode_batch(handmade_batch()))
+    b = ds.gen_batch(20240615, 300, 1, 1 << 12, density=(0.01, 0.9))
+    check_bsr_batch(ctx, orc, ds.bsr_encode_batch(b))
+
+
+def test_batch_bsr_device_arrays_and_capacity(ctx, orc):
+    import torch
+    bb = ds.bsr_encode_batch(ds.gen_batch(20240616, 500, 16, 1 << 13, density=(0.5, 0.5)))
+    want = expected_bsr(orc, bb)
+    t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).view(dt)).cuda()  # noqa: E731
+    bases, states = t(bb.bases, np.int32), t(bb.states, np.int32)
+    arrs = [t(x, np.int64) for x in (bb.a_off, bb.a_len, bb.b_off, bb.b_len)]
+    n = len(bb)
+    caps = np.minimum(bb.a_len, bb.b_len)
+    cap = int(caps.sum())
+    offs = np.zeros(n, np.uint64)
+    offs[1:] = np.cumsum(caps[:-1])
+    ob = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+    os_ = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+    lens = torch.zeros(n, dtype=torch.int64, device="cuda")
+    ctx.check(_lib.lib.setops_gpu_batch_intersect_bsr(
+        ctx.handle, bases.data_ptr(), states.data_ptr(), bases.numel(),
+        *[a.data_ptr() for a in arrs], n, ob.data_ptr(), os_.data_ptr(), cap, None,
+        lens.data_ptr(), 0))
+    hb, hs, hl = (ob.cpu().numpy().view(np.uint32), os_.cpu().numpy().view(np.uint32),
+                  lens.cpu().numpy())
+    for p, (wb, ws) in enumerate(want):
+        lo, m = int(offs[p]), int(hl[p])
+        assert m == wb.size and np.array_equal(hb[lo:lo + m], wb) and np.array_equal(hs[lo:lo + m], ws), p
+    rc = _lib.lib.setops_gpu_batch_intersect_bsr(
+        ctx.handle, bases.data_ptr(), states.data_ptr(), bases.numel(),
+        *[a.data_ptr() for a in arrs], n, ob.data_ptr(), os_.data_ptr(), cap - 1, None,
+        lens.data_ptr(), 0)
+    assert rc == _lib.ERR_CAPACITY
