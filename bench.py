@@ -371,6 +371,7 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
     t_batch = sorted(ts)[len(ts) // 2]
     matches = int(lens.sum().item())
     alg = 4 * int(b.pool.size) + 4 * matches
+    steady = steady_state(ctx, stream, L, pool, arrs, npairs, out, cap, doffs, lens)
     # the plain path: one launch per pair (async C-ABI on device pointers)
     ns = min(npairs, 3000)
     out2 = torch.empty(max(int(caps[:ns].sum()), 1), dtype=torch.int32, device="cuda")
@@ -412,7 +413,61 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
                                 "api": "setops_gpu_intersect_async per pair, device pointers"},
         "speedup_vs_one_launch_per_pair": (npairs / t_batch) / (ns / t_pp),
         "results_match_per_pair_path": True,
+        "steady_state": steady,
     }
+
+
+def steady_state(ctx, stream, L, pool, arrs, npairs, out, cap, doffs, lens) -> dict:
+    """Steady-state launches: a batch plan (the batch captured once in a CUDA
+    graph) replayed back to back, against repeated plain batch calls on the
+    same device arrays (each call: offset scan, capacity read-back, launch).
+    For the whole batch and for its first 1,000 pairs.  Replays must give the
+    plain call's results."""
+    import ctypes as C
+
+    import torch
+
+    res = {"api": "setops_gpu_batch_plan_create / _launch vs setops_gpu_batch_intersect"}
+    for label, n in (("full", npairs), ("small", min(1000, npairs))):
+        reps = 5 if label == "full" else 50
+        sub_cap = cap if n == npairs else int(doffs[n].item())
+        plan = C.c_void_p()
+        ctx.check(L.setops_gpu_batch_plan_create(
+            ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+            out.data_ptr(), sub_cap, None, lens.data_ptr(), C.byref(plan)))
+        try:
+            ctx.check(L.setops_gpu_batch_plan_launch(plan))
+            ctx.check(L.setops_gpu_synchronize(ctx.handle))
+            ref_out = out[:sub_cap].clone()
+            ref_lens = lens[:n].clone()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                ctx.check(L.setops_gpu_batch_plan_launch(plan))
+            e1.record(stream)
+            e1.synchronize()
+            ctx.check(L.setops_gpu_synchronize(ctx.handle))
+            t_graph = e0.elapsed_time(e1) * 1e-3 / reps
+        finally:
+            ctx.check(L.setops_gpu_batch_plan_destroy(plan))
+
+        def plain():
+            ctx.check(L.setops_gpu_batch_intersect(
+                ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+                out.data_ptr(), sub_cap, None, lens.data_ptr(), 0))
+        plain()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            plain()
+        torch.cuda.synchronize()
+        t_plain = (time.perf_counter() - t0) / reps
+        if not (torch.equal(ref_lens, lens[:n]) and torch.equal(ref_out, out[:sub_cap])):
+            raise SystemExit(f"graph replay of the {label} batch differs from the plain call")
+        res[label] = {"pairs": n, "replays": reps, "graph_ms": 1e3 * t_graph,
+                      "plain_call_ms": 1e3 * t_plain, "graph_pairs_per_s": n / t_graph,
+                      "speedup": t_plain / t_graph, "results_equal": True}
+    return res
 
 
 BSR_SEED = 20240617

@@ -211,6 +211,25 @@ int setops_gpu_batch_count_bsr(setops_ctx *ctx, const uint32_t *bases, const uin
                                size_t pool_len, const uint64_t *a_off, const uint64_t *a_len,
                                const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
                                uint64_t *counts, unsigned flags);
+/* Steady-state replay.  A batch on DEVICE arrays captured once into a CUDA
+ * graph (the offset scan when out_off is NULL, then the batch kernel, with
+ * the context's batch policy at creation) and replayed by plan_launch on the
+ * context's stream: no host work or synchronisation per replay.  The caller
+ * may rewrite the arrays' contents between replays (same pointers, same
+ * npairs).  The output capacity is checked on the device; an overflowing
+ * pair records SETOPS_ERR_CAPACITY (reported by the next synchronising call,
+ * e.g. setops_gpu_synchronize) and gets length 0.  out == NULL captures the
+ * count form.  The plan owns its coordination words and offsets, so other
+ * calls on the context may run between replays (not concurrently).  No
+ * counterpart in the reference; it replaces a loop of batch calls. */
+typedef struct setops_batch_plan setops_batch_plan;
+int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                                 const uint64_t *a_off, const uint64_t *a_len,
+                                 const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                                 uint32_t *out, size_t out_cap, const uint64_t *out_off,
+                                 uint64_t *out_lens, setops_batch_plan **plan);
+int setops_gpu_batch_plan_launch(setops_batch_plan *plan);
+int setops_gpu_batch_plan_destroy(setops_batch_plan *plan);
 /* Autotuner: times every kernel shape with several search ratios on the
  * given sample batch (materialising, `reps` timed runs each) and keeps the
  * fastest as the batch policy.  Plays the role of the reference's per-ISA

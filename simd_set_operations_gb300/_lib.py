@@ -83,6 +83,9 @@ SIGNATURES = [
     ("setops_gpu_batch_intersect_bsr", C.c_int,
      [vp, vp, vp, sz, vp, vp, vp, vp, sz, vp, vp, sz, vp, vp, uint]),
     ("setops_gpu_batch_count_bsr", C.c_int, [vp, vp, vp, sz, vp, vp, vp, vp, sz, vp, uint]),
+    ("setops_gpu_batch_plan_create", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, sz, vp, vp, vp]),
+    ("setops_gpu_batch_plan_launch", C.c_int, [vp]),
+    ("setops_gpu_batch_plan_destroy", C.c_int, [vp]),
     ("setops_gpu_batch_set_policy", C.c_int, [vp, C.c_int, C.c_uint32]),
     ("setops_gpu_batch_get_policy", C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint32)]),
     ("setops_gpu_batch_num_variants", C.c_int, []),

@@ -262,6 +262,15 @@ int batch_bsr_impl(setops_ctx *ctx, const uint32_t *bases, const uint32_t *state
 
 }  // namespace
 
+// A batch captured once into a CUDA graph and replayed (see setops_gpu.h).
+struct setops_batch_plan {
+  setops_ctx *ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void *dmem = nullptr;  // the plan's own coordination words and offsets
+  int kernels = 0;       // kernel launches per replay
+};
+
 // The batch kernel of a shape (for callers launching on their own stream).
 const KernelInfo &batch_kernel_info(bool mat, int variant) {
   if (variant < 0 || variant >= kNumBatch) variant = 0;
@@ -305,6 +314,101 @@ int setops_gpu_batch_count_bsr(setops_ctx *ctx, const uint32_t *bases, const uin
                                uint64_t *counts, unsigned flags) {
   return batch_bsr_impl(ctx, bases, states, pool_len, a_off, a_len, b_off, b_len, npairs,
                         nullptr, nullptr, 0, nullptr, counts, flags);
+}
+
+int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t pool_len,
+                                 const uint64_t *a_off, const uint64_t *a_len,
+                                 const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                                 uint32_t *out, size_t out_cap, const uint64_t *out_off,
+                                 uint64_t *out_lens, setops_batch_plan **plan_out) {
+  if (!ctx || !plan_out) return SETOPS_ERR_INVALID;
+  *plan_out = nullptr;
+  (void)pool_len;
+  if (npairs == 0 || !pool || !a_off || !a_len || !b_off || !b_len || !out_lens)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "batch plan: NULL array or no pairs");
+  CK(cudaSetDevice(ctx->device));
+  const bool mat = out != nullptr;
+  const bool scan = mat && !out_off;
+  auto *plan = new setops_batch_plan;
+  plan->ctx = ctx;
+  const size_t sync_bytes = 256;  // LaunchSync, padded
+  const size_t bytes = sync_bytes + (scan ? npairs * 8 + 8 : 0);
+  cudaError_t e = cudaMalloc(&plan->dmem, bytes);
+  if (e == cudaSuccess) e = cudaMemset(plan->dmem, 0, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(plan->dmem);
+    delete plan;
+    return ctx_cuda(ctx, e, "batch plan scratch");
+  }
+  LaunchSync *sync = static_cast<LaunchSync *>(plan->dmem);
+  uint64_t *offs = reinterpret_cast<uint64_t *>(static_cast<char *>(plan->dmem) + sync_bytes);
+  const KernelInfo &k = kBatchU32[ctx->batch_variant][mat ? 1 : 0];
+  int occ = 1;
+  int rc = ctx_occupancy(ctx, k, &occ);
+  if (rc == SETOPS_OK) {
+    const uint64_t grid =
+        std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, npairs));
+    BatchArgs a{};
+    a.pool = pool;
+    a.a_off = a_off;
+    a.a_len = a_len;
+    a.b_off = b_off;
+    a.b_len = b_len;
+    a.npairs = npairs;
+    a.out_off = scan ? offs : out_off;
+    a.out = out;
+    a.out_lens = out_lens;
+    a.search_ratio = ctx->batch_search_ratio;
+    a.out_cap = mat ? std::max<uint64_t>(out_cap, 1) : 0;  // checked per pair on the device
+    a.sync = sync;
+    a.err = ctx->derr;
+    void *args[] = {&a};
+    // capture: (offset scan) + batch kernel, on the context's stream
+    e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      if (scan)
+        batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(a_len, b_len, npairs, offs,
+                                                            offs + npairs);
+      cudaError_t le = cudaGetLastError();
+      if (le == cudaSuccess)
+        le = cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args, k.dyn_smem, ctx->st);
+      e = cudaStreamEndCapture(ctx->st, &plan->graph);
+      if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+    if (e != cudaSuccess) rc = ctx_cuda(ctx, e, "batch plan capture");
+  }
+  if (rc != SETOPS_OK) {
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    cudaFree(plan->dmem);
+    delete plan;
+    return rc;
+  }
+  plan->kernels = scan ? 2 : 1;
+  *plan_out = plan;
+  return SETOPS_OK;
+}
+
+int setops_gpu_batch_plan_launch(setops_batch_plan *plan) {
+  if (!plan) return SETOPS_ERR_INVALID;
+  setops_ctx *ctx = plan->ctx;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaGraphLaunch(plan->exec, ctx->st));
+  ctx->launches += uint64_t(plan->kernels);
+  return SETOPS_OK;
+}
+
+int setops_gpu_batch_plan_destroy(setops_batch_plan *plan) {
+  if (!plan) return SETOPS_OK;
+  setops_ctx *ctx = plan->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->st);  // no replay in flight
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  cudaFree(plan->dmem);
+  delete plan;
+  return SETOPS_OK;
 }
 
 int setops_gpu_batch_set_policy(setops_ctx *ctx, int variant, uint32_t search_ratio) {

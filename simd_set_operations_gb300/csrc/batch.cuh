@@ -38,6 +38,7 @@ struct BatchArgs {
   uint32_t *out;            // output pool (materialise)
   uint64_t *out_lens;       // per pair: intersection length
   uint32_t search_ratio;    // pairs with max/min >= this take the search path; 0 = never
+  uint64_t out_cap;         // materialise: checked on the device when non-zero (graph replays)
   LaunchSync *sync;
   int *err;
 };
@@ -120,6 +121,13 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchArgs p) {
     if (na > nb) {
       const uint32_t *tp = A; A = B; B = tp;
       const uint64_t tn = na; na = nb; nb = tn;
+    }
+    if (MAT && p.out_cap && p.out_off[k] + na > p.out_cap) {  // (na: the smaller length)
+      if (t == 0) {
+        record_error(p.err, DEV_ERR_CAPACITY);
+        p.out_lens[k] = 0;
+      }
+      continue;
     }
     uint32_t *dst = MAT ? p.out + p.out_off[k] : nullptr;
     uint64_t r = 0;

@@ -203,3 +203,63 @@ def test_batch_bsr_device_arrays_and_capacity(ctx, orc):
         *[a.data_ptr() for a in arrs], n, ob.data_ptr(), os_.data_ptr(), cap - 1, None,
         lens.data_ptr(), 0)
     assert rc == _lib.ERR_CAPACITY
+
+
+# ---- steady-state replay (CUDA graph) ---------------------------------------
+
+def test_batch_plan_replays(ctx, orc, generated):
+    """A plan captured once replays the batch exactly, again after its inputs
+    were rewritten in place, in count form too; an overflowing output is
+    reported by the next synchronising call."""
+    import torch
+    want = expected(orc, generated)
+    t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).view(dt)).cuda()  # noqa: E731
+    pool = t(generated.pool, np.int32)
+    arrs = [t(x, np.int64) for x in (generated.a_off, generated.a_len, generated.b_off,
+                                     generated.b_len)]
+    n = len(generated)
+    caps = np.minimum(generated.a_len, generated.b_len)
+    cap = int(caps.sum())
+    offs = np.zeros(n, np.uint64)
+    offs[1:] = np.cumsum(caps[:-1])
+    out = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+    lens = torch.zeros(n, dtype=torch.int64, device="cuda")
+    plan = C.c_void_p()
+    ctx.check(_lib.lib.setops_gpu_batch_plan_create(
+        ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+        out.data_ptr(), cap, None, lens.data_ptr(), C.byref(plan)))
+    try:
+        def check(shift):
+            ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+            o, ln = out.cpu().numpy().view(np.uint32), lens.cpu().numpy()
+            for p, w in enumerate(want):
+                lo, m = int(offs[p]), int(ln[p])
+                assert m == w.size and np.array_equal(o[lo:lo + m], w + np.uint32(shift)), p
+        for _ in range(3):
+            out.fill_(-1)
+            lens.zero_()
+            ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+            check(0)
+        # new contents, same shape: every value + 1000 (order and matches keep)
+        pool.add_(1000)
+        ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+        check(1000)
+        pool.sub_(1000)
+    finally:
+        ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
+    # count form
+    counts = torch.zeros(n, dtype=torch.int64, device="cuda")
+    ctx.check(_lib.lib.setops_gpu_batch_plan_create(
+        ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+        None, 0, None, counts.data_ptr(), C.byref(plan)))
+    ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+    ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+    ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
+    assert [int(c) for c in counts.cpu().numpy()] == [w.size for w in want]
+    # capacity checked on the device
+    ctx.check(_lib.lib.setops_gpu_batch_plan_create(
+        ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+        out.data_ptr(), cap - 1, None, lens.data_ptr(), C.byref(plan)))
+    ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+    assert _lib.lib.setops_gpu_synchronize(ctx.handle) == _lib.ERR_CAPACITY
+    ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
