@@ -73,6 +73,7 @@ def parse():
     p.add_argument("--batch-pairs", type=int, default=100000)
     p.add_argument("--bsr-pairs", type=int, default=10000,
                    help="pairs of the BSR subset of the batch leg")
+    p.add_argument("--no-kset", action="store_true", help="skip the k-set leg")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving leg (k-set queries against a resident index)")
     p.add_argument("--serve-rates", default="10000,50000,200000,1000000",
@@ -559,6 +560,62 @@ def batch_bsr_leg(ctx, stream, npairs: int) -> dict:
     }
 
 
+KSET_SEED = 20240618
+
+
+def kset_leg(ctx, stream, ks=(3, 5, 8)) -> dict:
+    """The reference's k-set configuration: k sorted sets with |S_1| = 2^22
+    and Zipf sizes |S_i| = 2^22 / i (exponent 1.0, the reference's skewness
+    factor 1000 in thousandths), element space
+    2^22 / 0.2, a core of 5 % of the smallest set in every set, intersected
+    smallest-first (svs_generic, setops/src/intersect/svs.rs:50-73) with the
+    intermediates on the device: setops_gpu_svs on device pointers, CUDA
+    events over back-to-back calls.  Algorithmic bytes: every set read once
+    plus the output written."""
+    import ctypes as C
+
+    import torch
+
+    from simd_set_operations_gb300 import _lib, datasets as ds
+    L = _lib.lib
+    peak, _ = read_peak()
+    rows = []
+    for k in ks:
+        sets = ds.gen_kset(KSET_SEED + k, 0.2, 0.05, 1 << 22, 1.0, k)  # Zipf exponent 1.0
+        dsets = [torch.from_numpy(x.view(np.int32)).cuda() for x in sets]
+        ptrs = (C.c_void_p * k)(*[d.data_ptr() for d in dsets])
+        lens = (C.c_size_t * k)(*[int(x.size) for x in sets])
+        cap = min(int(x.size) for x in sets)
+        out = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+        n_out = C.c_size_t()
+
+        def run():
+            ctx.check(L.setops_gpu_svs(ctx.handle, ptrs, lens, k, out.data_ptr(), out.numel(),
+                                       C.byref(n_out), 0))
+        for _ in range(3):
+            run()
+        reps = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3 / reps
+        nin = sum(int(x.size) for x in sets)
+        alg = 4 * nin + 4 * int(n_out.value)
+        core = int(0.05 * min(int(x.size) for x in sets))
+        if int(n_out.value) < core:
+            raise SystemExit(f"k={k}: {n_out.value} results, below the {core}-element core")
+        rows.append({"k": k, "sizes": [int(x.size) for x in sets], "out": int(n_out.value),
+                     "ms": 1e3 * t, "kset_per_s": 1.0 / t, "GBps_algorithmic": alg / t / 1e9,
+                     "frac_of_peak": alg / t / 1e9 / peak})
+    return {"workload": "k-set SvS: k in {3, 5, 8}, |S_i| = 2^22 / i, density 0.2, core 5 % of "
+                        "the smallest set, u32, materialised, smallest first; inputs resident",
+            "api": "setops_gpu_svs, device pointers (each call waits for its result length)",
+            "rows": rows}
+
+
 SERVE_SEED = 20240612
 
 
@@ -814,6 +871,9 @@ def run_gb300(args):
     if rank == 0 and not args.no_batch:
         batch = batch_leg(ctx, stream, args.batch_pairs)
         batch["bsr_subset"] = batch_bsr_leg(ctx, stream, args.bsr_pairs)
+    kset = None
+    if rank == 0 and not args.no_kset:
+        kset = kset_leg(ctx, stream)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_leg(ctx, [int(x) for x in args.serve_rates.split(",")])
@@ -825,7 +885,7 @@ def run_gb300(args):
         "data": "synthetic (seeded; reference generator shape)",
         "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "batch": batch,
+        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "batch": batch, "kset": kset,
         "serve": serve,
         "timing": {"bracket_ms_total": wall_ms, "kernel_ms_total": dev_ms,
                    "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
