@@ -90,13 +90,34 @@ def dist_env():
     return rank, world, local
 
 
+def sweep_seeds(rank: int) -> list[int]:
+    """Seeds of a rank's sweep pairs: every rank (replica) intersects its own
+    pairs of the same shapes; rank 0's are the single-GPU workload."""
+    return [SEED + 1000 * rank + k for k in range(len(SMALL_EXPS))]
+
+
 def make_sweep(rank: int):
     from simd_set_operations_gb300 import datasets as ds
-    pairs = []
-    for k, e in enumerate(SMALL_EXPS):
-        s, l = ds.gen_twoset(SEED + 1000 * rank + k, DENSITY, SELECTIVITY, 1 << e, LARGE)
-        pairs.append((s, l))
-    return pairs
+    return [ds.gen_twoset(sd, DENSITY, SELECTIVITY, 1 << e, LARGE)
+            for sd, e in zip(sweep_seeds(rank), SMALL_EXPS)]
+
+
+def max_over_ranks(x: float) -> float:
+    """The largest x over the ranks (a timed region's length: the job ends
+    with its slowest rank); x itself without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, pairs_per_step: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: the pairs every rank intersected over the
+    slowest rank's time (weak scaling: per-rank work fixed)."""
+    return world * pairs_per_step * steps / seconds
 
 
 def algorithmic_bytes(ns: int, nl: int, nout: int) -> int:
@@ -774,13 +795,8 @@ def run_gb300(args):
                 for i in range(len(pairs))]
     dev_ms = sum(sum(p) for p in per_pair)
     wall_ms = t_start.elapsed_time(t_end)
-    el_s = wall_ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([el_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_s = float(t.item())
-    value = world * len(pairs) * args.steps / el_s
+    el_s = max_over_ranks(wall_ms / 1e3)
+    value = job_value(world, len(pairs), args.steps, el_s)
 
     # roofline: the headline kernel (the 2^24 x 2^24 pair; size ratio 1 -> tiled bitmap)
     head = max(range(len(pairs)), key=lambda i: pairs[i][0].size)
@@ -835,14 +851,10 @@ def run_gb300(args):
             tot_out = step_e2e()
         e_el = time.perf_counter() - t0
         barrier()
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([e_el], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_el = float(t.item())
+        e_el = max_over_ranks(e_el)
         h2d = sum(4 * (s.size + l.size) for s, l in pairs)
         d2h = 4 * tot_out + 8 * len(pairs)
-        e2e = {"value": world * len(pairs) * e2e_steps / e_el, "unit": UNIT,
+        e2e = {"value": job_value(world, len(pairs), e2e_steps, e_el), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "ms_per_step": 1e3 * e_el / e2e_steps,
                "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers"}
