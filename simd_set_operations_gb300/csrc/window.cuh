@@ -24,10 +24,13 @@
 //      window, b moves past them, and when the whole window was used the
 //      next window follows.  An element above alast is read again by the
 //      next tile (from L2; it was just loaded);
-//   3. count mode counts; materialise mode marks matches in bitmap M (in
-//      value order) and appends the tile's matches, in order, to the CTA's
-//      staging run, which starts at the CTA's first A index (an exclusive
-//      region);
+//   3. count mode counts; materialise mode appends each window's matches,
+//      in B's order (= value order), to the CTA's staging run, which starts
+//      at the CTA's first A index (an exclusive region): each warp reads a
+//      contiguous part of the window, so a ballot per load round places a
+//      lane's matches within its warp and the warps' match totals, exchanged
+//      at the window's barrier, place the warps -- no bitmap of matches and
+//      no extraction pass;
 //   4. T is cleared.
 //
 // So a tile costs two rounds of loads (A, then B) and no search, and every
@@ -55,10 +58,8 @@ struct WindowCfg {
   static_assert((VW & (VW - 1)) == 0 && VW >= kTile, "a sparse tile (+6 end elements) fits T");
   static constexpr uint32_t kSpan = uint32_t(VW) * 32u;
   static constexpr int kTabWords = VW + 8;
-  static constexpr int kMWords = MAT ? VW : 0;
-  static constexpr int kSWords = MAT ? VW / 32 : 0;  // summary: one bit per M word
-  static_assert(VW / 32 <= NT && (VW / 32) % 4 == 0, "one summary word per thread");
-  static constexpr size_t kSmemBytes = size_t(kTabWords + kMWords + kSWords) * 4;
+  static_assert(UB * 4 <= 30, "a thread's window hits fit one mask word");
+  static constexpr size_t kSmemBytes = size_t(kTabWords) * 4;
 };
 
 template <int NT, int UA, int UB, int VW, int MINB, bool MAT>
@@ -69,12 +70,10 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
   constexpr uint32_t TA = Cfg::kTile;
 
   extern __shared__ __align__(128) uint32_t smem[];
-  uint32_t *tab = smem;                    // T (dense) or the sorted A tile (sparse)
-  uint32_t *mbits = smem + Cfg::kTabWords; // M: matches of the tile (materialise)
-  uint32_t *sbits = mbits + Cfg::kMWords;  // S: M words holding a match
+  uint32_t *tab = smem;  // T (dense) or the sorted A tile (sparse)
   __shared__ unsigned long long s_b0;
-  __shared__ uint32_t s_le[3];  // B elements of a window up to alast (rotating)
-  __shared__ uint32_t warp_sums[NW];
+  __shared__ uint32_t s_le[3];      // B elements of a window up to alast (rotating)
+  __shared__ uint32_t s_wt[3][NW];  // materialise: matches of each warp in a window
   __shared__ unsigned long long red[NW];
 
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
   const uint64_t ca0 = nb ? uint64_t(blockIdx.x) * na / G : 0;
   const uint64_t ca1 = nb ? (uint64_t(blockIdx.x) + 1) * na / G : 0;
 
-  for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords + Cfg::kSWords) / 4; i += NT)
+  for (int i = t; i < Cfg::kTabWords / 4; i += NT)
     reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
   if (t < 3) s_le[t] = 0;
   __syncthreads();  // T zero before any thread inserts
@@ -205,35 +204,22 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
     // so b may stop up to three elements short of the first element above
     // alast.  Those elements are below the next tile's first value: probed
     // again, they match nothing.
-    auto mark = [&](uint32_t o) {  // a match at M bit o (rare)
-      atomicOr(&mbits[o >> 5], 1u << (o & 31));
-      atomicOr(&sbits[o >> 10], 1u << ((o >> 5) & 31));
-    };
-    auto probe_dense = [&](uint32_t x) {
+    //
+    // Warp w takes a contiguous part of the window body, UB*32 16-byte
+    // words.  Count mode: round u, lane l loads word u*32 + l of it (32
+    // consecutive words per warp load).  Materialise mode: lane l loads words
+    // l*UB .. l*UB + UB-1 (consecutive for the lane; the strided warp loads
+    // go through L1, so each sector still comes from L2 once), so the
+    // window's elements are in the order (head, warp, lane, element, tail),
+    // which is B's order.  Matches are written in that order straight to the
+    // staging run: one bit-plane ballot scan of the lanes' match counts
+    // places them within the warp, and the warps' totals (exchanged at the
+    // window's barrier) place the warps.
+    auto probe_dense = [&](uint32_t x) -> uint32_t {
       const uint32_t o = min(x - w, span + 1);
-      const uint32_t hit = __funnelshift_r(tab[o >> 5], 0u, o) & 1u;
-      if (MAT) {
-        if (hit) mark(o);
-      } else {
-        cnt += hit;
-      }
+      return __funnelshift_r(tab[o >> 5], 0u, o) & 1u;
     };
-    // materialise, dense: four probes, then one branch for the (rare) hits
-    auto probe4_dense_mat = [&](const uint4 &v) {
-      const uint32_t o0 = min(v.x - w, span + 1), o1 = min(v.y - w, span + 1);
-      const uint32_t o2 = min(v.z - w, span + 1), o3 = min(v.w - w, span + 1);
-      const uint32_t h = (__funnelshift_r(tab[o0 >> 5], 0u, o0) & 1u) |
-                         ((__funnelshift_r(tab[o1 >> 5], 0u, o1) & 1u) << 1) |
-                         ((__funnelshift_r(tab[o2 >> 5], 0u, o2) & 1u) << 2) |
-                         ((__funnelshift_r(tab[o3 >> 5], 0u, o3) & 1u) << 3);
-      if (h) {
-        if (h & 1u) mark(o0);
-        if (h & 2u) mark(o1);
-        if (h & 4u) mark(o2);
-        if (h & 8u) mark(o3);
-      }
-    };
-    auto probe_sparse = [&](uint32_t x) {
+    auto probe_sparse = [&](uint32_t x) -> uint32_t {
       uint32_t lo = 0, len = nt;
       while (len > 0) {
         const uint32_t hh = len >> 1;
@@ -244,10 +230,7 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
           len = hh;
         }
       }
-      if (lo < nt && tab[lo] == x) {  // M bit by A position
-        if (MAT) mark(lo);
-        else ++cnt;
-      }
+      return (lo < nt && tab[lo] == x) ? 1u : 0u;
     };
     for (;;) {
       if (b >= nb) break;
@@ -261,113 +244,122 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
       // the tail after the last whole word belongs to the window only when
       // the window reaches B's end
       const uint64_t we = (qe == nbq) ? nb : bodyend;
-      const uint4 *wq = B4 + qa;
       const uint32_t nq = uint32_t(qe - qa);
+      const uint32_t wb0 = uint32_t(warp) * uint32_t(UB * 32);  // this warp's first word
+      const uint4 *wq = B4 + qa + wb0;
       const bool full = nq == uint32_t(UB * NT);
+      // word of round u within the warp's part
+      auto wi = [&](int u) -> uint32_t {
+        return MAT ? uint32_t(lane * UB + u) : uint32_t(u * 32 + lane);
+      };
       uint32_t le = 0;  // elements up to alast: head / tail one by one, words x4
-      {
-        uint4 vb[UB];
-        if (full) {
+      uint32_t hm = 0;  // materialise: bit 4u + k = element k of round u matched; bit 30 = xe
+      uint4 vb[UB];
+      auto ld = [&](int u) { return MAT ? __ldg(wq + wi(u)) : __ldcs(wq + wi(u)); };
+      if (full) {
 #pragma unroll
-          for (int u = 0; u < UB; ++u) vb[u] = __ldcs(wq + (u * NT + t));
-        } else {
+        for (int u = 0; u < UB; ++u) vb[u] = ld(u);
+      } else {
 #pragma unroll
-          for (int u = 0; u < UB; ++u)
-            vb[u] = uint32_t(u * NT + t) < nq ? __ldcs(wq + (u * NT + t)) : make_uint4(0, 0, 0, 0);
-        }
-        const uint32_t nh = uint32_t(ha - b), ntl = uint32_t(we - bodyend);
-        const bool is_h = uint32_t(t) < nh;
-        const bool is_t = uint32_t(t) >= 32 && uint32_t(t) < 32 + ntl;
-        uint32_t xe = 0;
-        if (is_h) xe = __ldg(B + b + t);
-        else if (is_t) xe = __ldg(B + bodyend + (t - 32));
-        auto run = [&](auto probe, auto probe4) {
-          auto p4 = [&](const uint4 &v) {
-            probe4(v);
-            le += v.w <= alast ? 4u : 0u;
-          };
-          if (full) {
-#pragma unroll
-            for (int u = 0; u < UB; ++u) p4(vb[u]);
-          } else {
-#pragma unroll
-            for (int u = 0; u < UB; ++u)
-              if (uint32_t(u * NT + t) < nq) p4(vb[u]);
-          }
-          if (is_h || is_t) {
-            probe(xe);
-            le += xe <= alast ? 1u : 0u;
-          }
-        };
-        auto each4 = [](auto probe) {
-          return [probe](const uint4 &v) {
-            probe(v.x);
-            probe(v.y);
-            probe(v.z);
-            probe(v.w);
-          };
-        };
-        if (dense) {
-          if (MAT) run(probe_dense, probe4_dense_mat);
-          else run(probe_dense, each4(probe_dense));
-        } else {
-          run(probe_sparse, each4(probe_sparse));
-        }
+        for (int u = 0; u < UB; ++u) vb[u] = wb0 + wi(u) < nq ? ld(u) : make_uint4(0, 0, 0, 0);
       }
+      // head elements on warp 0, tail elements on the last warp
+      const uint32_t nh = uint32_t(ha - b), ntl = uint32_t(we - bodyend);
+      const bool is_h = warp == 0 && uint32_t(lane) < nh;
+      const bool is_t = warp == NW - 1 && uint32_t(lane) < ntl;
+      uint32_t xe = 0;
+      if (is_h) xe = __ldg(B + b + lane);
+      else if (is_t) xe = __ldg(B + bodyend + lane);
+      auto run = [&](auto probe) {
+#pragma unroll
+        for (int u = 0; u < UB; ++u) {
+          if (full || wb0 + wi(u) < nq) {
+            const uint4 v = vb[u];
+            const uint32_t h = probe(v.x) | (probe(v.y) << 1) | (probe(v.z) << 2) | (probe(v.w) << 3);
+            if (MAT) hm |= h << (4 * u);
+            else cnt += uint32_t(__popc(h));
+            le += v.w <= alast ? 4u : 0u;
+          }
+        }
+        if (is_h || is_t) {
+          const uint32_t h = probe(xe);
+          if (MAT) hm |= h << 30;
+          else cnt += h;
+          le += xe <= alast ? 1u : 0u;
+        }
+      };
+      if (dense) run(probe_dense);
+      else run(probe_sparse);
       // one barrier per window: slot wc%3 sums this window; the slot of two
       // windows on is cleared (its last readers passed this barrier)
       le = __reduce_add_sync(0xffffffffu, le);
       if (lane == 0 && le) atomicAdd(&s_le[wc % 3], le);
+      if (MAT) {
+        const uint32_t wt = __reduce_add_sync(0xffffffffu, uint32_t(__popc(hm)));
+        if (lane == 0) s_wt[wc % 3][warp] = wt;
+      }
       __syncthreads();
       const uint32_t used = s_le[wc % 3];
+      if (MAT) {
+        uint32_t before = 0, wtot = 0;  // matches of the warps before this one; of all
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+          const uint32_t x = s_wt[wc % 3][q];
+          before += (q < warp) ? x : 0u;
+          wtot += x;
+        }
+        uint64_t o = staged + before;  // this warp's next output position
+        const uint32_t lt = (1u << lane) - 1u;
+        // one segment's matches: lane counts c (< 32) scanned over the warp by
+        // bit-plane ballots; all lanes of the warp call it
+        auto place = [&](uint32_t c, uint32_t &ex, uint32_t &tot) {
+          ex = 0;
+          tot = 0;
+#pragma unroll
+          for (int bit = 0; bit < 5; ++bit) {
+            const unsigned pl = __ballot_sync(0xffffffffu, (c >> bit) & 1u);
+            ex += uint32_t(__popc(pl & lt)) << bit;
+            tot += uint32_t(__popc(pl)) << bit;
+          }
+        };
+        uint32_t ex, tot;
+        if (warp == 0) {  // head first
+          const uint32_t hh = is_h ? (hm >> 30) & 1u : 0u;
+          const unsigned pl = __ballot_sync(0xffffffffu, hh);
+          if (hh) dst[o + uint32_t(__popc(pl & lt))] = xe;
+          o += uint32_t(__popc(pl));
+        }
+        const uint32_t hb = hm & ((1u << (4 * UB)) - 1u);  // body matches, lane order
+        place(uint32_t(__popc(hb)), ex, tot);
+        {
+          uint64_t q = o + ex;
+#pragma unroll
+          for (int u = 0; u < UB; ++u) {
+            const uint4 v = vb[u];
+            const uint32_t h = (hb >> (4 * u)) & 0xFu;
+            if (h & 1u) dst[q++] = v.x;
+            if (h & 2u) dst[q++] = v.y;
+            if (h & 4u) dst[q++] = v.z;
+            if (h & 8u) dst[q++] = v.w;
+          }
+        }
+        o += tot;
+        if (warp == NW - 1) {  // tail last
+          const uint32_t th = is_t ? (hm >> 30) & 1u : 0u;
+          const unsigned pl = __ballot_sync(0xffffffffu, th);
+          if (th) dst[o + uint32_t(__popc(pl & lt))] = xe;
+        }
+        staged += wtot;
+      }
       if (t == 0) s_le[(wc + 2) % 3] = 0;
       ++wc;
       b += used;
       if (b < we) break;  // an element above alast: the tile is done
     }
 
-    // ---- 3. output (materialise) and clearing ----
-    const uint32_t mw = dense ? (span >> 5) + 1 : (nt + 31) / 32;  // M / T words in use
-    if (MAT) {
-      // thread t < sw owns summary word t, i.e. M words [32t, 32t + 32):
-      // counts its matches, takes its place by a block scan, writes them
-      const uint32_t sw = (mw + 31) / 32;
-      const uint32_t sv = uint32_t(t) < sw ? sbits[t] : 0u;
-      uint32_t pc = 0;
-      for (uint32_t r = sv; r; r &= r - 1) pc += __popc(mbits[32u * t + uint32_t(__ffs(r) - 1)]);
-      uint32_t incl = pc;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      if (lane == 31) warp_sums[warp] = incl;
-      __syncthreads();
-      uint32_t before = 0, tot = 0;
-#pragma unroll
-      for (int q = 0; q < NW; ++q) {
-        const uint32_t sm = warp_sums[q];
-        before += (q < warp) ? sm : 0u;
-        tot += sm;
-      }
-      uint64_t q = staged + before + incl - pc;
-      for (uint32_t r = sv; r; r &= r - 1) {
-        const uint32_t i = 32u * t + uint32_t(__ffs(r) - 1);
-        uint32_t m = mbits[i];
-        mbits[i] = 0;
-        while (m) {
-          const uint32_t bit = i * 32u + uint32_t(__ffs(m) - 1);
-          m &= m - 1;
-          dst[q++] = dense ? w + bit : tab[bit];
-        }
-      }
-      if (sv) sbits[t] = 0;
-      staged += tot;
-      __syncthreads();  // sparse: the table was read above; warp sums reused
-    }
+    // ---- 3. clear T (dense: the words used; sparse: the tile) ----
     {
-      // clear T (dense: the words used; sparse: the tile)
-      const uint32_t tw = dense ? mw : nt;
+      const uint32_t tw = dense ? (span >> 5) + 1 : nt;
       for (uint32_t i = uint32_t(t); i < tw; i += NT) tab[i] = 0;
     }
     __syncthreads();  // T clear before the next tile's insertion
