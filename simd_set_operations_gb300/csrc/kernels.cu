@@ -6,6 +6,7 @@
 #include "merge.cuh"
 #include "tile.cuh"
 #include "window.cuh"
+#include "kset.cuh"
 
 namespace setops {
 
@@ -106,6 +107,19 @@ constexpr int count_of(const T (&)[N]) {
 }
 
 }  // namespace
+
+// NT threads, A tiles of 4*4*NT = 2048 elements, windows of 4*5*NT, bitmaps
+// of 4096 words (dense tiles span < 131,072 values), 6 CTAs/SM
+const KernelInfo &kset_kernel(bool mat) {
+  static const KernelInfo k[2] = {
+      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 5, 4096, 6, false>),
+                 kKsetThreads, KsetCfg<kKsetThreads, 4, 5, 4096, false>::kSmemBytes,
+                 KsetCfg<kKsetThreads, 4, 5, 4096, false>::kTile, "kset_count"},
+      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 5, 4096, 6, true>),
+                 kKsetThreads, KsetCfg<kKsetThreads, 4, 5, 4096, true>::kSmemBytes,
+                 KsetCfg<kKsetThreads, 4, 5, 4096, true>::kTile, "kset_mat", true}};
+  return k[mat ? 1 : 0];
+}
 
 int num_variants(Algo algo, bool bsr) {
   if (algo == ALGO_MERGE) return bsr ? count_of(kMergeBsr) : count_of(kMergeU32);

@@ -28,6 +28,9 @@ struct KernelInfo {
 enum Algo { ALGO_MERGE = 1, ALGO_GALLOP = 2, ALGO_BITMAP = 3 };
 
 int num_variants(Algo algo, bool bsr);
+// The fused k-set kernel (kset.cuh): count or materialise.
+const KernelInfo &kset_kernel(bool mat);
+constexpr int kKsetThreads = 128;
 // kind: 0 count, 1 materialise
 const KernelInfo &variant(Algo algo, bool bsr, bool mat, int v);
 

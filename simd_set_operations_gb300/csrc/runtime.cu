@@ -12,6 +12,7 @@
 #include "../../include/setops_gpu.h"
 #include "gallop.cuh"
 #include "kernels.h"
+#include "kset.cuh"
 #include "merge.cuh"
 #include "runtime.h"
 
@@ -789,6 +790,45 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
   if (host && mat) {
     RK(buf_reserve(ctx, ctx->out0, mn * 4));
     final_out = static_cast<uint32_t *>(ctx->out0.p);
+  }
+  uint64_t *lens_dev0 = &ctx->dlen[2];
+  // k >= 3 sets of sizes within 16x of the smallest: one fused launch reads
+  // every set once and keeps the survivors in shared memory (kset.cuh)
+  if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && k >= 3 && k <= size_t(kKsetMax) &&
+      lens[order[k - 1]] / mn < 16) {
+    const KernelInfo &kk = kset_kernel(mat);
+    int occ = 1;
+    RK(ctx_occupancy(ctx, kk, &occ));
+    const uint64_t ntiles = (mn + kk.tile - 1) / kk.tile;
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, ntiles));
+    RK(ctx_status_words(ctx, grid));
+    KsetArgs a{};
+    for (size_t i = 0; i < k; ++i) {
+      a.sets[i] = d[order[i]];
+      a.lens[i] = lens[order[i]];
+    }
+    a.k = int(k);
+    if (mat) {
+      RK(buf_reserve(ctx, ctx->stage0, mn * 4));
+      a.stage = static_cast<uint32_t *>(ctx->stage0.p);
+      a.out = final_out;
+      a.out_cap = out_cap;
+    }
+    a.out_len = lens_dev0;
+    a.coranks = static_cast<uint64_t *>(ctx->status.p);
+    a.sync = ctx->sync;
+    a.err = ctx->derr;
+    void *args[] = {&a};
+    RK(ctx_launch(ctx, kk, grid, args));
+    ++ctx->launches;
+    uint64_t n = 0;
+    RK(ctx_read_u64(ctx, lens_dev0, &n));  // (also reports device-side errors)
+    if (host && mat && n > 0) {
+      CK(cudaMemcpyAsync(out, final_out, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaStreamSynchronize(ctx->st));
+    }
+    *len_host = n;
+    return SETOPS_OK;
   }
   RK(buf_reserve(ctx, ctx->inter[0], mn * 4));
   RK(buf_reserve(ctx, ctx->inter[1], mn * 4));

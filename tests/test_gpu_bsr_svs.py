@@ -137,3 +137,12 @@ def test_svs_device_pointers(ctx, orc):
     w = so.VecWriter()
     so.gpu_svs(tsets, w, ctx=ctx)
     assert np.array_equal(w.into(), want)
+
+
+@pytest.mark.parametrize("k,dens", [(3, 0.001), (6, 0.3), (16, 0.05), (4, 0.9)])
+def test_svs_fused_shapes(ctx, orc, k, dens):
+    """Sets within 16x of the smallest take the fused k-set kernel: sparse
+    tiles (density 0.001), dense ones, the most sets it takes (16)."""
+    sets = ds.gen_kset(600 + k, dens, 0.1, 1 << 18, 0.5, k)
+    want = check_svs(ctx, orc, sets)
+    assert want.size >= int(0.1 * min(s.size for s in sets))
