@@ -163,6 +163,13 @@ int setops_gpu_svs(setops_ctx *ctx, const uint32_t *const *sets,
 int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
                          const size_t *lens, size_t k, uint64_t *count,
                          unsigned flags);
+/* Device arrays only, no synchronisation: the result length goes to the
+ * device word *len_dev (like setops_gpu_intersect_async); errors surface at
+ * setops_gpu_synchronize().  out == NULL: the count goes to *len_dev.  The
+ * set pointer and length arrays are host arrays (read during the call). */
+int setops_gpu_svs_async(setops_ctx *ctx, const uint32_t *const *sets,
+                         const size_t *lens, size_t k, uint32_t *out,
+                         size_t out_cap, uint64_t *len_dev, unsigned flags);
 
 /* ---- batched 2-set --------------------------------------------------------
  * Many independent pairs in one launch.  Replaces a loop of Intersect2 /

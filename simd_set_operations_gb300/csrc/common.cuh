@@ -152,6 +152,25 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
       : "memory");
 }
 
+// Asks the L2 to fetch global [p, p + bytes) ahead of the loads that will
+// read it (1-D bulk prefetch: no registers, nothing to wait for).  p and
+// bytes must be multiples of 16 and the range inside the allocation.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Prefetch (as above) of the whole 16-byte words [q0, q1) of x4, clipped to
+// [qlo, qhi) (the words wholly inside the array), in pieces of 64 KB.
+__device__ __forceinline__ void prefetch_words_l2(const uint4 *x4, uint64_t q0, uint64_t q1,
+                                                  uint64_t qlo, uint64_t qhi) {
+  q0 = q0 > qlo ? q0 : qlo;
+  q1 = q1 < qhi ? q1 : qhi;
+  for (; q0 < q1; q0 += 4096) {
+    const uint64_t n = (q1 - q0 < 4096) ? q1 - q0 : 4096;
+    bulk_prefetch_l2(x4 + q0, uint32_t(n) * 16u);
+  }
+}
+
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;"

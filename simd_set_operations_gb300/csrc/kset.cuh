@@ -91,17 +91,32 @@ __global__ void __launch_bounds__(NT, MINB) kset_kernel(const KsetArgs p) {
   const uint64_t amis = (reinterpret_cast<uintptr_t>(A) >> 2) & 3;
   const uint4 *A4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(A) & ~uintptr_t(15));
 
-  // cursors: set j's first element >= A[ca0]; warps take sets in turn
+  // cursors: set j's first element >= A[ca0]; warps take sets in turn.
+  // A CTA's chain of dependent loads (searches, tiles, windows) is long
+  // next to its work, so everything it will read is first requested into L2:
+  // its S0 run, and each set's range between the guesses for the run's first
+  // and last values (with a margin); the chain then waits on L2, not HBM.
   if (ntiles) {
-    const uint32_t key = __ldg(A + ca0);
+    const uint32_t key = __ldg(A + ca0), klast = __ldg(A + ca1 - 1);
+    if (t == NT - 1)
+      prefetch_words_l2(A4, (amis + ca0) >> 2, ((amis + ca1) >> 2) + 1, amis ? 1 : 0,
+                        (amis + na) >> 2);
     for (int j = 1 + warp; j < k; j += NW) {
       const uint32_t *B = p.sets[j];
       const uint64_t nb = p.lens[j];
       const uint32_t bfirst = __ldg(B), blast = __ldg(B + nb - 1);
-      const uint64_t est =
-          (blast <= bfirst || key <= bfirst)
-              ? 0
-              : uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
+      auto guess = [&](uint32_t v) -> uint64_t {
+        return (blast <= bfirst || v <= bfirst)
+                   ? 0
+                   : uint64_t(double(v - bfirst) / double(blast - bfirst) * double(nb - 1));
+      };
+      const uint64_t est = guess(key);
+      if (lane == 0) {
+        const uint64_t bmis = (reinterpret_cast<uintptr_t>(B) >> 2) & 3;
+        const uint4 *B4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(B) & ~uintptr_t(15));
+        const uint64_t q0 = (bmis + est) >> 2, q1 = ((bmis + guess(klast)) >> 2) + 1;
+        prefetch_words_l2(B4, q0 > 512 ? q0 - 512 : 0, q1 + 512, bmis ? 1 : 0, (bmis + nb) >> 2);
+      }
       const uint64_t r = warp_lower_bound(B, nb, key, est);
       if (lane == 0) s_b[j] = r;
     }

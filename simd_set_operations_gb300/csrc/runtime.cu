@@ -743,9 +743,12 @@ int setops_gpu_bsr_to_sorted(setops_ctx *ctx, const uint32_t *bases,
 
 // ---- k-set SvS ----
 
+// len_dev != NULL: asynchronous form (device arrays only): the result length
+// goes to the device word *len_dev and nothing waits for the GPU.
 static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
                     const size_t *lens, size_t k, uint32_t *out,
-                    size_t out_cap, uint64_t *len_host, unsigned flags) {
+                    size_t out_cap, uint64_t *len_host, unsigned flags,
+                    uint64_t *len_dev = nullptr) {
   if (!ctx) return SETOPS_ERR_INVALID;
   if (!sets || !lens || k < 2)
     return ctx_fail(ctx, SETOPS_ERR_INVALID, "svs needs k >= 2 sets");
@@ -764,8 +767,15 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
   const uint64_t mn = lens[order[0]];
   if (mat && out_cap < mn)
     return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap < smallest set");
+  if (len_dev && host)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "the asynchronous k-set call takes device arrays");
   if (mn == 0) {
-    *len_host = 0;
+    if (len_dev) {
+      CK(cudaSetDevice(ctx->device));
+      CK(cudaMemsetAsync(len_dev, 0, sizeof(uint64_t), ctx->st));
+    } else {
+      *len_host = 0;
+    }
     return SETOPS_OK;
   }
   CK(cudaSetDevice(ctx->device));
@@ -814,13 +824,14 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
       a.out = final_out;
       a.out_cap = out_cap;
     }
-    a.out_len = lens_dev0;
+    a.out_len = len_dev ? len_dev : lens_dev0;
     a.coranks = static_cast<uint64_t *>(ctx->status.p);
     a.sync = ctx->sync;
     a.err = ctx->derr;
     void *args[] = {&a};
     RK(ctx_launch(ctx, kk, grid, args));
     ++ctx->launches;
+    if (len_dev) return SETOPS_OK;  // errors surface at the next synchronising call
     uint64_t n = 0;
     RK(ctx_read_u64(ctx, lens_dev0, &n));  // (also reports device-side errors)
     if (host && mat && n > 0) {
@@ -884,6 +895,11 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
     }
     ub = std::min(ub, nb);
   }
+  if (len_dev) {
+    CK(cudaMemcpyAsync(len_dev, &lens_dev[k - 2], sizeof(uint64_t), cudaMemcpyDeviceToDevice,
+                       ctx->st));
+    return SETOPS_OK;
+  }
   uint64_t n = 0;
   RK(ctx_read_u64(ctx, &lens_dev[k - 2], &n));
   if (host && mat && n > 0) {
@@ -904,6 +920,13 @@ int setops_gpu_svs(setops_ctx *ctx, const uint32_t *const *sets,
                     &n, flags);
   if (rc == SETOPS_OK) *out_len = size_t(n);
   return rc;
+}
+
+int setops_gpu_svs_async(setops_ctx *ctx, const uint32_t *const *sets,
+                         const size_t *lens, size_t k, uint32_t *out,
+                         size_t out_cap, uint64_t *len_dev, unsigned flags) {
+  if (!len_dev) return ctx_fail(ctx, SETOPS_ERR_INVALID, "len_dev is NULL");
+  return svs_impl(ctx, sets, lens, k, out, out_cap, nullptr, flags, len_dev);  // out NULL: count
 }
 
 int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,

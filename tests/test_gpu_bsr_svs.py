@@ -146,3 +146,31 @@ def test_svs_fused_shapes(ctx, orc, k, dens):
     sets = ds.gen_kset(600 + k, dens, 0.1, 1 << 18, 0.5, k)
     want = check_svs(ctx, orc, sets)
     assert want.size >= int(0.1 * min(s.size for s in sets))
+
+
+def test_svs_async(ctx, orc):
+    """setops_gpu_svs_async: the result (or the count) on the device, no
+    synchronisation; the fused path and the step-wise path (a set over 16x
+    the smallest)."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from simd_set_operations_gb300 import _lib
+    rng = np.random.default_rng(33)
+    for sizes in ((40_000, 90_000, 120_000, 60_000), (10_000, 400_000, 30_000)):
+        sets = sorted([rand_set(rng, n, 1 << 21) for n in sizes], key=len)
+        want = orc.svs_generic(sets)
+        ts = [torch.from_numpy(s.view(np.int32)).cuda() for s in sets]
+        ptrs = (C.c_void_p * len(ts))(*[x.data_ptr() for x in ts])
+        lens = (C.c_size_t * len(ts))(*[s.size for s in sets])
+        out = torch.full((sets[0].size,), -1, dtype=torch.int32, device="cuda")
+        dlen = torch.zeros(1, dtype=torch.int64, device="cuda")
+        for _ in range(2):
+            ctx.check(_lib.lib.setops_gpu_svs_async(ctx.handle, ptrs, lens, len(ts), out.data_ptr(),
+                                                    out.numel(), dlen.data_ptr(), 0))
+        ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+        n = int(dlen.item())
+        assert n == want.size and np.array_equal(out[:n].cpu().numpy().view(np.uint32), want)
+        ctx.check(_lib.lib.setops_gpu_svs_async(ctx.handle, ptrs, lens, len(ts), None, 0,
+                                                dlen.data_ptr(), 0))
+        ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+        assert int(dlen.item()) == want.size
