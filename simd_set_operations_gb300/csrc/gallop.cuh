@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
   __shared__ uint32_t sSt[(MAT && BSR) ? TILE : 1];
   __shared__ uint32_t warp_sums[NT / 32];
   __shared__ uint32_t s_vid;
-  __shared__ unsigned long long s_excl;
+  __shared__ uint32_t s_last;
   __shared__ unsigned long long red[NT / 32];
 
   const int t = threadIdx.x;
@@ -318,27 +318,74 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
     }
     return;
   }
-  if (t < 32) {
-    const uint64_t ex = lookback_exclusive_warp(p.status, vid, cta_cnt, p.epoch, p.err);
-    if (t == 0) {
-      s_excl = ex;
-      if (ex != UINT64_MAX && ex + cta_cnt > p.out_cap)
-        record_error(p.err, DEV_ERR_CAPACITY);
-    }
+  // Placement.  Each CTA publishes its match count (p.status[vid]); the last
+  // CTA to get here turns the counts into offsets (an exclusive scan, in
+  // place, the total in p.status[G]) and raises the flag sync->acc = 1 that
+  // the others wait for (the launch is cooperative: all CTAs are resident).
+  // Then every CTA copies its staged run.  Matches are few on the pairs that
+  // take this kernel, and CTAs finish in any order: a chained look-back would
+  // wait on the slowest predecessor once per CTA.
+  if (t == 0) {
+    p.status[vid] = cta_cnt;
+    __threadfence();
+    s_last = atomicAdd(&p.sync->done, 1u) == G - 1 ? 1u : 0u;
   }
   __syncthreads();
-  const uint64_t ex = s_excl;
-  if (ex == UINT64_MAX || ex + cta_cnt > p.out_cap) return;
-  for (uint64_t q = t; q < cta_cnt; q += NT) {
-    p.out[ex + q] = p.stage[s0 + q];
-    if (BSR) p.out_s[ex + q] = p.stage_s[s0 + q];
-  }
-  if (t == 0) {
-    if (vid == G - 1) *p.out_len = ex + cta_cnt;
+  if (s_last) {
     __threadfence();
-    if (atomicAdd(&p.sync->done, 1u) == G - 1) {
+    const uint32_t per_t = (G + NT - 1) / NT;  // thread t scans [t*per_t, t*per_t + per_t)
+    const uint32_t i0 = uint32_t(t) * per_t, i1 = (i0 + per_t < G) ? i0 + per_t : G;
+    uint32_t sum = 0;
+    for (uint32_t i = i0; i < i1; ++i) sum += uint32_t(p.status[i]);
+    uint32_t tot;
+    uint64_t run_off = block_exclusive_scan<NT>(sum, warp_sums, &tot);
+    for (uint32_t i = i0; i < i1; ++i) {
+      const uint64_t c = p.status[i];
+      p.status[i] = run_off;
+      run_off += c;
+    }
+    if (t == 0) {
+      p.status[G] = tot;
+      if (tot > p.out_cap) record_error(p.err, DEV_ERR_CAPACITY);
+      else *p.out_len = tot;
+      __threadfence();
+      atomicExch(&p.sync->acc, 1ull);  // the flag
+    }
+    __syncthreads();
+  } else {
+    if (t == 0) {
+      uint32_t ok = 1;
+      const uint64_t t0 = global_ns();
+      while (ld_acquire_u64(reinterpret_cast<const uint64_t *>(&p.sync->acc)) == 0) {
+        __nanosleep(100);
+        if (global_ns() - t0 > kWaitLimitNs) {
+          record_error(p.err, DEV_ERR_TIMEOUT_LOOKBACK);
+          ok = 0;
+          break;
+        }
+      }
+      s_last = ok ? 0u : 2u;
+    }
+    __syncthreads();
+    if (s_last == 2u) return;  // timeout recorded
+  }
+  {
+    const uint64_t ex = p.status[vid], tot = p.status[G];
+    if (tot <= p.out_cap) {
+      for (uint64_t q = t; q < cta_cnt; q += NT) {
+        p.out[ex + q] = p.stage[s0 + q];
+        if (BSR) p.out_s[ex + q] = p.stage_s[s0 + q];
+      }
+    }
+  }
+  // the last CTA out resets the coordination words for the next launch
+  __syncthreads();
+  if (t == 0) {
+    __threadfence();
+    if (atomicAdd(&p.sync->acc, 1ull) == G) {
       p.sync->ticket = 0;
       p.sync->done = 0;
+      p.sync->acc = 0;
       __threadfence();
     }
   }

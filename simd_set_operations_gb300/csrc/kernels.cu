@@ -22,9 +22,10 @@ KernelInfo mk_merge(const char *name) {
 
 template <int NT, int GS, int ITEMS, int NSAMP, bool BSR, bool MAT>
 KernelInfo mk_gallop(const char *name) {
+  // materialise: cooperative (its placement waits on the last CTA's scan)
   return KernelInfo{reinterpret_cast<const void *>(
                         &gallop_kernel<NT, GS, ITEMS, NSAMP, BSR, MAT>),
-                    NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name};
+                    NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name, MAT};
 }
 
 template <int NT, int UA, int UB, int VW, int MINB, bool MAT>

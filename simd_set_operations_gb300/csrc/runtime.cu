@@ -220,11 +220,13 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
     // arrays: ratio < 4: tiled bitmap; 4..31: merge-path; 32..511: sampled
-    // thread-per-element search; 512..8191: 16 lanes per element; >= 8192: a
-    // warp per element.  BSR: merge-path below 32.
+    // thread-per-element search; 512..8191: 8 lanes per element (4 elements
+    // a warp); >= 8192: a warp per element.  BSR: merge-path below 32.
+    // (Measured on 2^10 / 2^14 / 2^18 x 2^24 pairs: each band's choice was
+    // the fastest variant there.)
     unsigned v = (b < 5)    ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
                  : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
-                 : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(1))
+                 : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3))
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
     unsigned u = (b < 2) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(0)) : v, s = v;
     ctx->policy[0][b] = u;
@@ -259,7 +261,7 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
   } else {
     const uint64_t ntiles = (mn + k.tile - 1) / k.tile;
     grid = std::max<uint64_t>(1, std::min(full, ntiles));
-    status_words = grid;
+    status_words = grid + 1;  // per-CTA counts, then the total
   }
   if (j.grid_cap && grid > j.grid_cap) grid = j.grid_cap;
   uint32_t epoch = 0;
