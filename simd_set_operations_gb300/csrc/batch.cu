@@ -55,13 +55,17 @@ struct BatchDev {
   const uint64_t *a_off, *a_len, *b_off, *b_len;
 };
 
-// One batched launch on device arrays.
+// One batched launch on device arrays.  unit_cap > 0: long pairs are split
+// over CTAs (room for unit_cap units; more: no splitting).
 int launch_batch(setops_ctx *ctx, const BatchDev &d, uint64_t npairs, uint32_t *out,
-                 const uint64_t *out_off, uint64_t *out_lens, int variant, uint32_t ratio) {
+                 const uint64_t *out_off, uint64_t *out_lens, int variant, uint32_t ratio,
+                 uint64_t unit_cap = 0) {
   const KernelInfo &k = kBatchU32[variant][out ? 1 : 0];
   int occ = 1;
   RK(ctx_occupancy(ctx, k, &occ));
-  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, npairs));
+  if (unit_cap) unit_cap = std::max<uint64_t>(unit_cap, npairs);
+  const uint64_t work = std::max<uint64_t>(npairs, unit_cap);  // tickets, at most
+  const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, work));
   BatchArgs a{};
   a.pool = d.pool;
   a.a_off = d.a_off;
@@ -75,6 +79,12 @@ int launch_batch(setops_ctx *ctx, const BatchDev &d, uint64_t npairs, uint32_t *
   a.search_ratio = ratio;
   a.sync = ctx->sync + 1;  // its own coordination slot
   a.err = ctx->derr;
+  if (unit_cap) {
+    RK(buf_reserve(ctx, ctx->units, prefix_bytes(npairs, unit_cap)));
+    launch_prefix(d.a_len, d.b_len, npairs, ctx->units.p, nullptr, nullptr, unit_cap, &a, ctx->st);
+    CK(cudaGetLastError());
+    ctx->launches += 2;
+  }
   void *args[] = {&a};
   return ctx_launch(ctx, k, grid, args);
 }
@@ -136,17 +146,33 @@ int batch_impl(setops_ctx *ctx, const uint32_t *pool, size_t pool_len, const uin
   } else if (mat && !out_off) {
     // device lengths: offsets by a device scan; its total is checked here
     RK(buf_reserve(ctx, ctx->in[5], npairs * 8));
+    RK(buf_reserve(ctx, ctx->units, prefix_bytes(npairs, 0)));
     uint64_t *o = static_cast<uint64_t *>(ctx->in[5].p);
-    batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(a_len, b_len, npairs, o, &ctx->dlen[1]);
+    launch_prefix(a_len, b_len, npairs, ctx->units.p, o, &ctx->dlen[1], 0, nullptr, ctx->st);
     CK(cudaGetLastError());
-    ++ctx->launches;
+    ctx->launches += 2;
     RK(ctx_read_u64(ctx, &ctx->dlen[1], &need));
     if (need > out_cap)
       return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap " + std::to_string(out_cap) +
                                                     " < " + std::to_string(need) + " output words");
     doff = o;
   }
-  RK(launch_batch(ctx, d, npairs, mat ? dout : nullptr, doff, dlens, v, ctx->batch_search_ratio));
+  // room for the unit map: exact when the lengths are on the host; from the
+  // output capacity on the device (materialise); else a guess (the map falls
+  // back to one unit per pair when the units do not fit)
+  uint64_t unit_cap = npairs > 0xFFFFFFFFull ? 0 : 2 * npairs + 4096;
+  if (host) {
+    uint64_t units = 0;
+    for (size_t q = 0; q < npairs; ++q) {
+      const uint64_t mn = std::min(a_len[q], b_len[q]);
+      units += mn > kBatchUnit ? (mn + kBatchUnit - 1) / kBatchUnit : 1;
+    }
+    unit_cap = unit_cap ? units : 0;
+  } else if (mat) {
+    unit_cap = unit_room(npairs, need ? need : out_cap);
+  }
+  RK(launch_batch(ctx, d, npairs, mat ? dout : nullptr, doff, dlens, v, ctx->batch_search_ratio,
+                  unit_cap));
   if (host) {
     if (mat && need) CK(cudaMemcpyAsync(out, dout, need * 4, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaMemcpyAsync(out_lens, dlens, npairs * 8, cudaMemcpyDeviceToHost, ctx->st));
@@ -239,10 +265,11 @@ int batch_bsr_impl(setops_ctx *ctx, const uint32_t *bases, const uint32_t *state
     CK(cudaStreamSynchronize(ctx->st));  // `offs` is a local
   } else if (mat && !out_off) {
     RK(buf_reserve(ctx, ctx->in[5], npairs * 8));
+    RK(buf_reserve(ctx, ctx->units, prefix_bytes(npairs, 0)));
     uint64_t *o = static_cast<uint64_t *>(ctx->in[5].p);
-    batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(a_len, b_len, npairs, o, &ctx->dlen[1]);
+    launch_prefix(a_len, b_len, npairs, ctx->units.p, o, &ctx->dlen[1], 0, nullptr, ctx->st);
     CK(cudaGetLastError());
-    ++ctx->launches;
+    ctx->launches += 2;
     RK(ctx_read_u64(ctx, &ctx->dlen[1], &need));
     if (need > out_cap)
       return ctx_fail(ctx, SETOPS_ERR_CAPACITY, "out_cap " + std::to_string(out_cap) +
@@ -332,7 +359,13 @@ int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t p
   auto *plan = new setops_batch_plan;
   plan->ctx = ctx;
   const size_t sync_bytes = 256;  // LaunchSync, padded
-  const size_t bytes = sync_bytes + (scan ? npairs * 8 + 8 : 0);
+  const size_t offs_bytes = scan ? ((npairs * 8 + 8 + 15) & ~size_t(15)) : 0;
+  // the unit map: room from the output capacity (materialise; it bounds the
+  // pairs' smaller lengths) or a guess (count; unsplit when it does not fit)
+  const uint64_t unit_cap = npairs > 0xFFFFFFFFull ? 0
+                            : mat                  ? unit_room(npairs, out_cap)
+                                                   : 2 * npairs + 4096;
+  const size_t bytes = sync_bytes + offs_bytes + prefix_bytes(npairs, unit_cap);
   cudaError_t e = cudaMalloc(&plan->dmem, bytes);
   if (e == cudaSuccess) e = cudaMemset(plan->dmem, 0, bytes);
   if (e != cudaSuccess) {
@@ -346,8 +379,8 @@ int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t p
   int occ = 1;
   int rc = ctx_occupancy(ctx, k, &occ);
   if (rc == SETOPS_OK) {
-    const uint64_t grid =
-        std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, npairs));
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, std::max<uint64_t>(unit_cap, npairs)));
     BatchArgs a{};
     a.pool = pool;
     a.a_off = a_off;
@@ -363,12 +396,12 @@ int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t p
     a.sync = sync;
     a.err = ctx->derr;
     void *args[] = {&a};
-    // capture: (offset scan) + batch kernel, on the context's stream
+    // capture: prefixes (offsets, unit map) + batch kernel, on the context's stream
     e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      if (scan)
-        batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(a_len, b_len, npairs, offs,
-                                                            offs + npairs);
+      if (scan || unit_cap)
+        launch_prefix(a_len, b_len, npairs, static_cast<char *>(plan->dmem) + sync_bytes + offs_bytes,
+                      scan ? offs : nullptr, offs + npairs, unit_cap, &a, ctx->st);
       cudaError_t le = cudaGetLastError();
       if (le == cudaSuccess)
         le = cudaLaunchKernel(k.fn, dim3(unsigned(grid)), dim3(k.nt), args, k.dyn_smem, ctx->st);
@@ -385,7 +418,7 @@ int setops_gpu_batch_plan_create(setops_ctx *ctx, const uint32_t *pool, size_t p
     delete plan;
     return rc;
   }
-  plan->kernels = scan ? 2 : 1;
+  plan->kernels = scan || unit_cap ? 3 : 1;
   *plan_out = plan;
   return SETOPS_OK;
 }
@@ -455,8 +488,9 @@ int setops_gpu_batch_autotune(setops_ctx *ctx, const uint32_t *pool, size_t pool
     CK(cudaStreamSynchronize(ctx->st));
   } else {
     RK(buf_reserve(ctx, ctx->in[5], npairs * 8));
-    batch_offsets_kernel<1024><<<1, 1024, 0, ctx->st>>>(
-        a_len, b_len, npairs, static_cast<uint64_t *>(ctx->in[5].p), &ctx->dlen[1]);
+    RK(buf_reserve(ctx, ctx->units, prefix_bytes(npairs, 0)));
+    launch_prefix(a_len, b_len, npairs, ctx->units.p, static_cast<uint64_t *>(ctx->in[5].p),
+                  &ctx->dlen[1], 0, nullptr, ctx->st);
     CK(cudaGetLastError());
     RK(ctx_read_u64(ctx, &ctx->dlen[1], &need));
   }

@@ -39,9 +39,18 @@ struct BatchArgs {
   uint64_t *out_lens;       // per pair: intersection length
   uint32_t search_ratio;    // pairs with max/min >= this take the search path; 0 = never
   uint64_t out_cap;         // materialise: checked on the device when non-zero (graph replays)
+  // Long pairs split into units (batch_prefix_*); NULL: one unit per pair.
+  const uint64_t *ustart;     // per pair: first unit; [npairs] = number of units
+  const uint32_t *unit_pair;  // per unit: its pair
+  uint64_t *ucount;           // per unit: its matches
+  uint32_t *pcount;           // per pair: units finished (zeroed by batch_prefix_global)
   LaunchSync *sync;
   int *err;
 };
+
+// Units of at most this many elements of a pair's smaller set: a longer pair
+// is intersected by several CTAs at once.
+constexpr uint64_t kBatchUnit = 16384;
 
 // Search path: for each element of A[0, na), a binary search of B[0, nb) in
 // global memory; hits are compacted in A order (ascending).  Returns the
@@ -109,12 +118,17 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchArgs p) {
   for (int i = t; i < (Cfg::kTabWords + Cfg::kMWords) / 4; i += NT)
     reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
 
+  const uint64_t nunits = p.ustart ? p.ustart[p.npairs] : p.npairs;
+  __shared__ uint32_t s_last;
   for (;;) {
     if (t == 0) s_pair = atomicAdd(&p.sync->ticket, 1u);
     __syncthreads();
-    const uint64_t k = s_pair;
+    const uint64_t un = s_pair;
     __syncthreads();  // everyone has read the ticket before it is reused
-    if (k >= p.npairs) break;
+    if (un >= nunits) break;
+    const uint64_t k = p.ustart ? p.unit_pair[un] : un;  // the pair
+    const uint64_t ju = p.ustart ? un - p.ustart[k] : 0;  // unit of the pair
+    const uint64_t nu = p.ustart ? p.ustart[k + 1] - p.ustart[k] : 1;
     uint64_t na = p.a_len[k], nb = p.b_len[k];
     const uint32_t *A = p.pool + p.a_off[k];
     const uint32_t *B = (p.pool_b ? p.pool_b : p.pool) + p.b_off[k];
@@ -129,28 +143,69 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchArgs p) {
       }
       continue;
     }
-    uint32_t *dst = MAT ? p.out + p.out_off[k] : nullptr;
+    // pair k, or unit ju of its nu units: A[s0, s1) against all of B, the
+    // matches at the same offset in the pair's output (a unit's own region)
+    const uint64_t s0 = ju * na / nu, s1 = (ju + 1) * na / nu;
+    uint32_t *dst = MAT ? p.out + p.out_off[k] + s0 : nullptr;
     uint64_t r = 0;
-    if (na > 0) {
+    if (s1 > s0) {
       if (p.search_ratio && nb / na >= p.search_ratio)
-        r = search_run<NT, MAT>(A, na, B, nb, dst, sh);
+        r = search_run<NT, MAT>(A + s0, s1 - s0, B, nb, dst, sh);
       else
-        r = tile_run<NT, TA, VW, MAT>(A, 0, na, B, nb, na > uint64_t(TA), dst, tab, mbits, sh);
+        r = tile_run<NT, TA, VW, MAT>(A, s0, s1, B, nb, nu > 1 || na > uint64_t(TA), dst, tab,
+                                      mbits, sh);
     }
-    if (!MAT) {
-      uint64_t v = r;
+    if (!MAT) {  // per-thread shares -> the total, in every thread
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp] = v;
+      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+      if (lane == 0) red[warp] = r;
       __syncthreads();
-      if (t == 0) {
-        uint64_t s = 0;
-        for (int q = 0; q < NW; ++q) s += red[q];
-        p.out_lens[k] = s;
-      }
-    } else if (t == 0) {
-      p.out_lens[k] = r;
+      r = 0;
+      for (int q = 0; q < NW; ++q) r += red[q];
     }
+    if (nu == 1) {
+      if (t == 0) p.out_lens[k] = r;
+      continue;  // (red is next written after the ticket's barriers)
+    }
+    // the last unit of the pair to finish packs the units' matches left, in
+    // unit order, and writes the pair's length
+    if (MAT) {
+      __threadfence();  // this thread's staged matches, before the count below
+      __syncthreads();
+    }
+    if (t == 0) {
+      p.ucount[un] = r;
+      __threadfence();
+      s_last = atomicAdd(&p.pcount[k], 1u) == uint32_t(nu - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      const uint64_t u0 = p.ustart[k];
+      uint64_t wpos = 0;  // packed length so far
+      for (uint64_t v = 0; v < nu; ++v) {
+        const uint64_t c = __ldcg(p.ucount + u0 + v);  // other CTAs' writes: not via L1
+        if (MAT) {
+          // move this unit's matches left, block by block: every read of a
+          // block before any write of it (the target is never right of the
+          // source, so later blocks are not overwritten)
+          const uint64_t src = v * na / nu;
+          uint32_t *o = p.out + p.out_off[k];
+          if (src != wpos) {
+            for (uint64_t b0 = 0; b0 < c; b0 += NT) {
+              const bool has = b0 + uint64_t(t) < c;
+              const uint32_t x = has ? __ldcg(o + src + b0 + t) : 0u;
+              __syncthreads();
+              if (has) o[wpos + b0 + t] = x;
+              __syncthreads();
+            }
+          }
+        }
+        wpos += c;
+      }
+      if (t == 0) p.out_lens[k] = wpos;
+    }
+    __syncthreads();  // s_last reused
   }
   // the last CTA out resets the ticket for the next launch
   if (t == 0) {
@@ -290,38 +345,182 @@ __global__ void __launch_bounds__(NT) batch_bsr_kernel(const BatchBsrArgs p) {
   }
 }
 
-// out_off[p] = sum of min(a_len, b_len) over pairs before p (one CTA).
+// ---- per-pair prefixes: output offsets and the unit map ----------------------
+// Two launches over chunks of NT pairs, one pair per thread (G = ceil(npairs /
+// NT) CTAs each): batch_prefix_local scans within a chunk and writes the chunk
+// sums; batch_prefix_global adds the sums of the chunks before it (each CTA
+// reads all G sums) and finishes the arrays.
+//   offsets (out_off != NULL): out_off[p] = sum of min(a_len, b_len) over the
+//     pairs before p, *out_total = the sum over all pairs;
+//   units (ustart != NULL): pair p gets nu = ceil(min / kBatchUnit) units (1
+//     for min <= kBatchUnit), ustart[p] = units before p, ustart[npairs] = all
+//     units, unit_pair[u] = the pair of unit u, pcount zeroed; when the units
+//     exceed unit_cap (the room in unit_pair) every pair gets one unit.
+
+__device__ __forceinline__ uint64_t batch_units_of(uint64_t mn) {
+  return mn > kBatchUnit ? (mn + kBatchUnit - 1) / kBatchUnit : 1;
+}
+
+// Exclusive 64-bit scan over the block; *total = the block's sum.
 template <int NT>
-__global__ void __launch_bounds__(NT) batch_offsets_kernel(const uint64_t *a_len,
-                                                           const uint64_t *b_len,
-                                                           uint64_t npairs, uint64_t *out_off,
-                                                           uint64_t *total) {
+__device__ __forceinline__ unsigned long long block_scan_u64(unsigned long long v,
+                                                             unsigned long long *ws,
+                                                             unsigned long long *total) {
   constexpr int NW = NT / 32;
-  __shared__ unsigned long long ws[NW];
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  unsigned long long base = 0;
-  for (uint64_t c0 = 0; c0 < npairs; c0 += NT) {
-    const uint64_t i = c0 + uint64_t(t);
-    const unsigned long long v = i < npairs ? (a_len[i] < b_len[i] ? a_len[i] : b_len[i]) : 0ull;
-    unsigned long long incl = v;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long x = v;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    if (lane == 31) ws[warp] = incl;
-    __syncthreads();
-    unsigned long long before = 0, tot = 0;
-#pragma unroll
-    for (int k = 0; k < NW; ++k) {
-      before += (k < warp) ? ws[k] : 0ull;
-      tot += ws[k];
-    }
-    if (i < npairs) out_off[i] = base + before + incl - v;
-    base += tot;
-    __syncthreads();
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  if (t == 0) *total = base;
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  unsigned long long before = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    const unsigned long long s = ws[w];
+    before += (w < warp) ? s : 0ull;
+    tot += s;
+  }
+  __syncthreads();  // ws reused by the next scan
+  *total = tot;
+  return before + x - v;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) batch_prefix_local(const uint64_t *a_len,
+                                                         const uint64_t *b_len, uint64_t npairs,
+                                                         uint64_t *out_off, uint64_t *osum,
+                                                         uint64_t *ustart, uint64_t *csum) {
+  __shared__ unsigned long long ws[NT / 32];
+  const uint64_t i = uint64_t(blockIdx.x) * NT + threadIdx.x;
+  const bool in = i < npairs;
+  const uint64_t mn = in ? (a_len[i] < b_len[i] ? a_len[i] : b_len[i]) : 0;
+  unsigned long long tot;
+  if (out_off) {
+    const unsigned long long x = block_scan_u64<NT>(mn, ws, &tot);
+    if (in) out_off[i] = x;
+    if (threadIdx.x == 0) osum[blockIdx.x] = tot;
+  }
+  if (ustart) {
+    const unsigned long long x = block_scan_u64<NT>(in ? batch_units_of(mn) : 0ull, ws, &tot);
+    if (in) ustart[i] = x;
+    if (threadIdx.x == 0) csum[blockIdx.x] = tot;
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) batch_prefix_global(
+    const uint64_t *a_len, const uint64_t *b_len, uint64_t npairs, uint64_t *out_off,
+    const uint64_t *osum, uint64_t *out_total, uint64_t *ustart, const uint64_t *csum,
+    uint32_t *unit_pair, uint32_t *pcount, uint64_t unit_cap) {
+  constexpr int NW = NT / 32;
+  __shared__ unsigned long long ws[4][NW];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t c = blockIdx.x, G = gridDim.x;
+  // [0] offsets before this chunk, [1] all offsets, [2] units before, [3] all units
+  unsigned long long s[4] = {0, 0, 0, 0};
+  for (uint32_t j = uint32_t(t); j < G; j += NT) {
+    const unsigned long long o = out_off ? osum[j] : 0ull, u = ustart ? csum[j] : 0ull;
+    s[0] += j < c ? o : 0ull;
+    s[1] += o;
+    s[2] += j < c ? u : 0ull;
+    s[3] += u;
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+    if (lane == 0) ws[q][warp] = s[q];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s[q] = 0;
+    for (int w = 0; w < NW; ++w) s[q] += ws[q][w];
+  }
+  const uint64_t i = uint64_t(c) * NT + uint64_t(t);
+  const bool in = i < npairs;
+  const bool last = c == G - 1 && t == 0;
+  if (out_off) {
+    if (in) out_off[i] += s[0];
+    if (last) *out_total = s[1];
+  }
+  if (ustart) {
+    const bool split = s[3] <= unit_cap;
+    if (in) {
+      pcount[i] = 0;
+      if (split) {
+        const uint64_t u0 = s[2] + ustart[i];
+        const uint64_t nv = batch_units_of(a_len[i] < b_len[i] ? a_len[i] : b_len[i]);
+        ustart[i] = u0;
+        for (uint64_t u = 0; u < nv; ++u) unit_pair[u0 + u] = uint32_t(i);
+      } else {
+        ustart[i] = i;
+        unit_pair[i] = uint32_t(i);
+      }
+    }
+    if (last) ustart[npairs] = split ? s[3] : npairs;
+  }
+}
+
+// ---- host side of the prefixes -------------------------------------------------
+
+constexpr int kPrefixNT = 1024;  // pairs per chunk of batch_prefix_*
+
+inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
+
+// Scratch of the per-pair prefixes: the chunk sums (2 x G words) and, with
+// unit_cap > 0, the unit map: ustart (npairs + 1), ucount and unit_pair
+// (unit_cap each), pcount (npairs); each part 16-byte aligned.
+inline size_t prefix_bytes(uint64_t npairs, uint64_t unit_cap) {
+  const uint64_t G = (npairs + kPrefixNT - 1) / kPrefixNT;
+  size_t b = 2 * a16(G * 8);
+  if (unit_cap)
+    b += a16((npairs + 1) * 8) + a16(unit_cap * 8) + a16(unit_cap * 4) + a16(npairs * 4);
+  return b;
+}
+
+// Room for the unit map when the pairs' smaller lengths sum to at most
+// `words`: a split pair of length m has at most m / kBatchUnit + 1 units.
+// 0 (no splitting) when a pair index does not fit unit_pair's 32 bits.
+inline uint64_t unit_room(uint64_t npairs, uint64_t words) {
+  return npairs > 0xFFFFFFFFull ? 0 : npairs + words / kBatchUnit + 1;
+}
+
+// Launches the prefixes of a batch on st (two launches, batch_prefix_*):
+// the output offsets when out_off is given (their total into *out_total) and
+// the unit map, carved from `scratch` into `a`, when unit_cap > 0 (room for
+// max(unit_cap, npairs) units).
+inline void launch_prefix(const uint64_t *a_len, const uint64_t *b_len, uint64_t npairs, void *scratch,
+                   uint64_t *out_off, uint64_t *out_total, uint64_t unit_cap, BatchArgs *a,
+                   cudaStream_t st) {
+  const uint64_t G = (npairs + kPrefixNT - 1) / kPrefixNT;
+  char *c = static_cast<char *>(scratch);
+  uint64_t *osum = reinterpret_cast<uint64_t *>(c);
+  c += a16(G * 8);
+  uint64_t *csum = reinterpret_cast<uint64_t *>(c);
+  c += a16(G * 8);
+  uint64_t *ustart = nullptr;
+  uint32_t *unit_pair = nullptr, *pcount = nullptr;
+  if (unit_cap) {
+    unit_cap = std::max<uint64_t>(unit_cap, npairs);
+    ustart = reinterpret_cast<uint64_t *>(c);
+    c += a16((npairs + 1) * 8);
+    a->ucount = reinterpret_cast<uint64_t *>(c);
+    c += a16(unit_cap * 8);
+    unit_pair = reinterpret_cast<uint32_t *>(c);
+    c += a16(unit_cap * 4);
+    pcount = reinterpret_cast<uint32_t *>(c);
+    a->ustart = ustart;
+    a->unit_pair = unit_pair;
+    a->pcount = pcount;
+  }
+  batch_prefix_local<kPrefixNT><<<unsigned(G), kPrefixNT, 0, st>>>(a_len, b_len, npairs, out_off,
+                                                                   osum, ustart, csum);
+  batch_prefix_global<kPrefixNT><<<unsigned(G), kPrefixNT, 0, st>>>(
+      a_len, b_len, npairs, out_off, osum, out_total, ustart, csum, unit_pair, pcount, unit_cap);
 }
 
 }  // namespace setops

@@ -64,6 +64,7 @@ struct setops_ctx {
   setops::DevBuf out0, out1;
   setops::DevBuf stage0, stage1;
   setops::DevBuf inter[2];
+  setops::DevBuf units;  // batch: the long-pair unit map
   uint32_t epoch = 1;
   uint64_t launches = 0;
   std::map<const void *, int> occ;
@@ -73,7 +74,7 @@ struct setops_ctx {
 
   std::vector<setops::DevBuf *> all_bufs() {
     std::vector<setops::DevBuf *> v = {&status, &out0, &out1, &stage0,
-                                       &stage1, &inter[0], &inter[1]};
+                                       &stage1, &inter[0], &inter[1], &units};
     for (auto &b : in) v.push_back(&b);
     return v;
   }

@@ -260,7 +260,14 @@ int launch(setops_srv *srv, int si) {
   const size_t off_roff = off_tab + align16(kMaxK * 8);
   const size_t off_i0 = off_roff + align16(nb8);
   const size_t off_i1 = off_i0 + align16(total * 4 + 16);
-  const size_t dbytes = off_i1 + align16(total * 4 + 16);
+  // long queries: each step's pairs split into units over CTAs (the map is
+  // rebuilt on the device per step; a step's smaller lengths are bounded by
+  // the queries' smallest lists)
+  uint64_t maxcap = 0;
+  for (uint32_t i = 0; i < n; ++i) maxcap = std::max(maxcap, cap[i]);
+  const uint64_t unit_cap = maxcap > kBatchUnit ? unit_room(n, total) : 0;
+  const size_t off_units = off_i1 + align16(total * 4 + 16);
+  const size_t dbytes = off_units + (unit_cap ? prefix_bytes(n, unit_cap) : 0);
   if (grow_device(s, dbytes)) return SETOPS_ERR_NOMEM;
   // mapped host results: counts, total, answers
   const size_t hr_bytes = align16(nb8) + 16 + align16(total * 4 + 16);
@@ -304,8 +311,13 @@ int launch(setops_srv *srv, int si) {
     a.search_ratio = ctx->batch_search_ratio;
     a.sync = ctx->sync + 2 + si;  // one coordination slot per batch slot
     a.err = ctx->derr;
+    if (unit_cap) {
+      launch_prefix(a.a_len, a.b_len, n, d + off_units, nullptr, nullptr, unit_cap, &a, st);
+      srv->launches += 2;
+    }
     void *args[] = {&a};
-    if (cudaLaunchKernel(srv->kfn, dim3(unsigned(std::min<uint64_t>(srv->grid, n))),
+    const uint64_t work = std::max<uint64_t>(n, unit_cap);
+    if (cudaLaunchKernel(srv->kfn, dim3(unsigned(std::min<uint64_t>(srv->grid, work))),
                          dim3(srv->knt), args, srv->ksmem, st) != cudaSuccess)
       return SETOPS_ERR_CUDA;
     ++srv->launches;

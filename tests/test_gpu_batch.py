@@ -133,6 +133,98 @@ def test_batch_autotune_keeps_results_exact(ctx, orc, generated):
         ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))
 
 
+def long_pairs_batch():
+    """Pairs whose smaller set spans several units of 16384 elements (split
+    over CTAs), at the unit boundary, identical (every element moves when the
+    units are packed), skewed, and mixed with small pairs."""
+    rng = np.random.default_rng(11)
+    same = rand_set(rng, 100000, 1 << 24)
+    sets = [
+        (rand_set(rng, 200000, 1 << 22), rand_set(rng, 300000, 1 << 22)),
+        (same, same.copy()),
+        (rand_set(rng, 16384, 1 << 16), rand_set(rng, 40000, 1 << 16)),
+        (rand_set(rng, 16385, 1 << 16), rand_set(rng, 40000, 1 << 16)),
+        (rand_set(rng, 3, 100), rand_set(rng, 50, 100)),
+        (rand_set(rng, 50000, 1 << 28), rand_set(rng, 2000000, 1 << 28)),
+        (np.empty(0, np.uint32), rand_set(rng, 70000, 1 << 20)),
+        (rand_set(rng, 70000, 1 << 18), rand_set(rng, 65536, 1 << 18)),
+    ]
+    pool = np.concatenate([np.concatenate([a, b]) for a, b in sets]).astype(np.uint32)
+    a_off, a_len, b_off, b_len = [], [], [], []
+    off = 0
+    for a, b in sets:
+        a_off.append(off); a_len.append(a.size); off += a.size
+        b_off.append(off); b_len.append(b.size); off += b.size
+    u = lambda x: np.array(x, np.uint64)  # noqa: E731
+    return ds.PairBatch(pool, u(a_off), u(a_len), u(b_off), u(b_len))
+
+
+def test_batch_long_pairs_split(ctx, orc):
+    """Long pairs split into units give the same results through host arrays
+    (exact unit count), device arrays (unit room from the output capacity)
+    and a replayed plan, for every search ratio."""
+    import torch
+    b = long_pairs_batch()
+    want = expected(orc, b)
+    v0, r0 = C.c_int(), C.c_uint32()
+    ctx.check(_lib.lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v0), C.byref(r0)))
+    t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x).view(dt)).cuda()  # noqa: E731
+    pool = t(b.pool, np.int32)
+    arrs = [t(x, np.int64) for x in (b.a_off, b.a_len, b.b_off, b.b_len)]
+    n = len(b)
+    caps = np.minimum(b.a_len, b.b_len)
+    cap = int(caps.sum())
+    offs = np.zeros(n, np.uint64)
+    offs[1:] = np.cumsum(caps[:-1])
+
+    def check_dev(out, lens):
+        o, ln = out.cpu().numpy().view(np.uint32), lens.cpu().numpy()
+        for p, w in enumerate(want):
+            lo, m = int(offs[p]), int(ln[p])
+            assert m == w.size and np.array_equal(o[lo:lo + m], w), p
+
+    try:
+        for v in range(_lib.lib.setops_gpu_batch_num_variants()):
+            for ratio in (0, 1, 16):
+                ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v, ratio))
+                check_batch(ctx, orc, b, want)
+                out = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+                lens = torch.zeros(n, dtype=torch.int64, device="cuda")
+                ctx.check(_lib.lib.setops_gpu_batch_intersect(
+                    ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+                    out.data_ptr(), cap, None, lens.data_ptr(), 0))
+                check_dev(out, lens)
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, 16))
+        out = torch.full((cap,), -1, dtype=torch.int32, device="cuda")
+        lens = torch.zeros(n, dtype=torch.int64, device="cuda")
+        plan = C.c_void_p()
+        ctx.check(_lib.lib.setops_gpu_batch_plan_create(
+            ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+            out.data_ptr(), cap, None, lens.data_ptr(), C.byref(plan)))
+        try:
+            for _ in range(3):
+                out.fill_(-1)
+                lens.zero_()
+                ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+                ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+                check_dev(out, lens)
+        finally:
+            ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
+        counts = torch.zeros(n, dtype=torch.int64, device="cuda")
+        ctx.check(_lib.lib.setops_gpu_batch_plan_create(
+            ctx.handle, pool.data_ptr(), pool.numel(), *[a.data_ptr() for a in arrs], n,
+            None, 0, None, counts.data_ptr(), C.byref(plan)))
+        try:
+            for _ in range(2):
+                ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
+                ctx.check(_lib.lib.setops_gpu_synchronize(ctx.handle))
+                assert [int(c) for c in counts.cpu().numpy()] == [w.size for w in want]
+        finally:
+            ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
+    finally:
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))
+
+
 # ---- BSR pairs ---------------------------------------------------------------
 
 def expected_bsr(orc, bb):

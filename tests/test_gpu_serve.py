@@ -73,3 +73,26 @@ def test_serve_rejects_bad_queries(ctx, index):
             srv.submit([1], 0)  # k < 2
         with pytest.raises(so.SetopsError):
             srv.submit([0, len(index)], 0)  # no such list
+
+
+def test_serve_long_lists_split(ctx, orc):
+    """Queries over lists longer than one unit (16384 elements), whose steps
+    are split over CTAs: answers equal svs_generic alone and batched."""
+    index = ds.gen_index(20240617, 3000, 1 << 17, 1.0, 1 << 21)
+    ids, ks = ds.gen_queries(20240618, 120, len(index), 2, 5, 1.3)
+    want = oracle_answers(orc, index, ids, ks)
+    assert max(int(min(index.lens[int(i)] for i in ids[q][:ks[q]])) for q in range(ks.size)) > 16384
+    with so.Server(index.pool, index.offs, index.lens, ctx=ctx) as srv:
+        for q in range(0, ks.size, 7):
+            srv.submit(ids[q][:ks[q]], q)
+            tag, res, _ = srv.wait(q)
+            assert tag == q and np.array_equal(res, want[q]), q
+        for q in range(ks.size):
+            srv.submit(ids[q][:ks[q]], 10_000 + q)
+        mix = {}
+        while len(mix) < ks.size:
+            r = srv.poll()
+            if r is not None:
+                mix[r[0] - 10_000] = r[1]
+        for q in range(ks.size):
+            assert np.array_equal(mix[q], want[q]), q
