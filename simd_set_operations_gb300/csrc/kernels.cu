@@ -6,6 +6,7 @@
 #include "merge.cuh"
 #include "tile.cuh"
 #include "window.cuh"
+#include "wwindow.cuh"
 #include "kset.cuh"
 
 namespace setops {
@@ -33,6 +34,13 @@ KernelInfo mk_window(const char *name) {
   using Cfg = WindowCfg<NT, UA, UB, VW, MAT>;
   return KernelInfo{reinterpret_cast<const void *>(&window_kernel<NT, UA, UB, VW, MINB, MAT>), NT,
                     Cfg::kSmemBytes, Cfg::kTile, name, MAT};
+}
+
+template <int NT, int UA, int UB, int VWW, int MINB, bool MAT>
+KernelInfo mk_wwindow(const char *name) {
+  using Cfg = WWindowCfg<NT, UA, UB, VWW, MAT>;
+  return KernelInfo{reinterpret_cast<const void *>(&wwindow_kernel<NT, UA, UB, VWW, MINB, MAT>),
+                    NT, Cfg::kSmemBytes, Cfg::kTile, name, MAT};
 }
 
 template <int NT, int TA, int VW, int MINB, bool MAT>
@@ -74,6 +82,9 @@ const KernelInfo kMergeBsr[][2] = {
 #define WINDOW_ROW(NT, UA, UB, VW, MINB)                                                     \
   {mk_window<NT, UA, UB, VW, MINB, false>("window_" #NT "_a" #UA "_b" #UB "_t" #VW "_m" #MINB), \
    mk_window<NT, UA, UB, VW, MINB, true>("window_" #NT "_a" #UA "_b" #UB "_t" #VW "_m" #MINB)}
+#define WWINDOW_ROW(NT, UA, UB, VWW, MINB)                                                       \
+  {mk_wwindow<NT, UA, UB, VWW, MINB, false>("wwindow_" #NT "_a" #UA "_b" #UB "_t" #VWW "_m" #MINB), \
+   mk_wwindow<NT, UA, UB, VWW, MINB, true>("wwindow_" #NT "_a" #UA "_b" #UB "_t" #VWW "_m" #MINB)}
 #define TILE_ROW(NT, TA, VW, MINB)                                             \
   {mk_tile<NT, TA, VW, MINB, false>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB), \
    mk_tile<NT, TA, VW, MINB, true>("bitmap_" #NT "_a" #TA "_t" #VW "_b" #MINB)}
@@ -83,6 +94,8 @@ const KernelInfo kBitmapU32[][2] = {
     WINDOW_ROW(256, 4, 5, 4096, 5),  // 2: 5 CTAs/SM
     WINDOW_ROW(256, 4, 4, 4096, 6),  // 3: 6 CTAs/SM
     TILE_ROW(256, 4096, 4096, 8),    // 4: tile kernel (a B search per tile)
+    WWINDOW_ROW(128, 4, 5, 512, 8),  // 5: warps on their own, 512-element tiles, 8 CTAs/SM
+    WWINDOW_ROW(1024, 4, 5, 512, 1), // 6: the same, one CTA of 32 warps per SM
 };
 
 // GS lanes per element (1 = thread per element with IT interleaved

@@ -6,10 +6,10 @@
 // Work layout
 // -----------
 // A is the smaller input.  CTA c of the G resident CTAs owns the run
-// A[c*na/G, (c+1)*na/G); its first B index b0 (the first B value >= the run's
-// first value) is found once, by one warp, while the other warps load the
-// first A tile.  Then, tile by tile (TA = 4*UA*NT elements of A, values
-// [w, alast]):
+// A[c*na/G, (c+1)*na/G); its first B index b0 (the first B value >= the
+// run's first value, or a little below it) is found once, by one warp, while
+// the other warps load the first A tile.  Then, tile by tile (TA = 4*UA*NT
+// elements of A, values [w, alast]):
 //
 //   1. every thread loads UA 16-byte words of the tile (all loads in flight
 //      at once) and sets their bits in bitmap T of the value range (dense:
@@ -108,15 +108,13 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
   const uint4 *A4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(A) & ~uintptr_t(15));
   const uint4 *B4 = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(B) & ~uintptr_t(15));
 
-  // warp 0: b0 = first B index with a value >= A[ca0]
+  // warp 0: b0 = where the run starts reading B, at or a little below the
+  // first B index with a value >= A[ca0] (B elements below A[ca0] match
+  // nothing in this run), from a guess at the same fraction of B as ca0 is
+  // of A
   if (ntiles && warp == 0) {
-    const uint32_t key = __ldg(A + ca0);
-    const uint32_t bfirst = __ldg(B), blast = __ldg(B + nb - 1);
-    const uint64_t est =
-        (blast <= bfirst || key <= bfirst)
-            ? 0
-            : uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
-    const uint64_t r = warp_lower_bound(B, nb, key, est);
+    const uint64_t est = uint64_t(double(ca0) / double(na) * double(nb));
+    const uint64_t r = warp_start_below(B, nb, A + ca0, est);
     if (lane == 0) s_b0 = r;
   }
 
