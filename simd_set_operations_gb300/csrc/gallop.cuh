@@ -10,9 +10,10 @@
 // once, so brackets come from cooperative searches instead:
 //   * each CTA owns a contiguous run of small elements (one static range per
 //     CTA, like the merge kernel's diagonal ranges);
-//   * NSAMP > 0: the CTA finds the large-set bracket of its whole run with
-//     two (NT+1)-ary block searches, then loads a shared-memory sample of NSAMP
-//     bracket maxima, so each element starts from a narrow block;
+//   * NSAMP > 0: the CTA bounds the large-set bracket of its whole run (two
+//     warps, one round of probes around a guess each; a few hundred elements
+//     of slack), then loads a shared-memory sample of NSAMP bracket maxima, so
+//     each element starts from a narrow block;
 //     NSAMP == 0: every element searches the whole large set (no per-CTA
 //     preparation; best when a CTA has few elements);
 //   * the search inside the block is either GS == 1: one thread per element,
@@ -60,6 +61,7 @@ struct GallopCfg {
                     GS == 32,
                 "group size must divide a warp");
   static_assert(GS == 1 || ITEMS == 1, "groups search one element at a time");
+  static_assert(NSAMP == 0 || NT >= 64, "two warps bound the run's bracket");
   static constexpr int kNG = NT / GS;
   static constexpr int kTile = kNG * ITEMS;  // elements per pass of a CTA
 };
@@ -76,31 +78,6 @@ __device__ __forceinline__ uint32_t smem_lower_bound(const uint32_t *samp,
     } else {
       len = half;
     }
-  }
-  return lo;
-}
-
-// CTA-cooperative lower_bound: first index in [lo, hi) with L[i] >= x (hi
-// if none).  Each round all NT threads probe evenly spaced points and the
-// bracket narrows (NT+1)-fold (3 rounds for 2^24 elements at NT = 256).
-// Call from every thread of the block with the same arguments.
-template <int NT>
-__device__ __forceinline__ uint64_t block_lower_bound(const uint32_t *L,
-                                                      uint64_t lo, uint64_t hi,
-                                                      uint32_t x) {
-  const int t = threadIdx.x;
-  while (hi > lo) {
-    const uint64_t span = hi - lo;
-    if (span <= uint64_t(NT)) {
-      const bool pr = uint64_t(t) < span && __ldg(L + lo + t) < x;
-      lo += uint64_t(__syncthreads_count(pr));
-      break;
-    }
-    const uint64_t xp = lo + (uint64_t(t + 1) * span) / (NT + 1);
-    const uint64_t c = uint64_t(__syncthreads_count(__ldg(L + xp) < x));
-    const uint64_t nhi = (c < uint64_t(NT)) ? lo + ((c + 1) * span) / (NT + 1) : hi;
-    if (c > 0) lo = lo + (c * span) / (NT + 1) + 1;
-    hi = nhi;
   }
   return lo;
 }
@@ -146,10 +123,22 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
   uint64_t st = 1;
   uint32_t nblk = 0;
   if (NSAMP > 0 && s1 > s0 && nl > 0) {
-    const uint32_t xf = __ldg(S + s0), xl = __ldg(S + s1 - 1);
-    blo = block_lower_bound<NT>(L, 0, nl, xf);
-    const uint64_t lbl = block_lower_bound<NT>(L, blo, nl, xl);
-    bhi = lbl < nl ? lbl + 1 : nl;  // lower_bound of the last is a candidate
+    // bounds, not exact indexes: warp 0 brackets the first element's
+    // lower_bound, warp 1 the last one's, at the same time (one round of
+    // probes each around a guess at the same fraction of L as of S)
+    __shared__ unsigned long long s_br[2];
+    const int warp = t >> 5;
+    if (warp < 2) {
+      const uint64_t i = warp == 0 ? s0 : s1 - 1;
+      const uint64_t est = uint64_t(double(i) / double(ns) * double(nl));
+      uint64_t lo, hi;
+      warp_bracket_guess(L, nl, S + i, est, &lo, &hi);
+      if (lane == 0) s_br[warp] = warp == 0 ? lo : hi;
+    }
+    __syncthreads();
+    blo = s_br[0];
+    const uint64_t lbl = s_br[1];   // at or above the last element's lower_bound
+    bhi = lbl < nl ? lbl + 1 : nl;  // which is a candidate
     const uint64_t len = bhi > blo ? bhi - blo : 0;
     st = len == 0 ? 1 : (len + SAMP - 1) / SAMP;
     nblk = len == 0 ? 0 : uint32_t((len + st - 1) / st);

@@ -103,115 +103,6 @@ __device__ __forceinline__ uint64_t warp_lower_bound(const uint32_t *__restrict_
   return lo + uint64_t(__popc(m));
 }
 
-// First index i in [0, n) with B[i] >= *keyp (n when none), n > 0; all lanes
-// of the calling warp take part and get the result, and the key in *key_out.
-// `est` guesses the index.  Round 1 loads the key together with 128 probes
-// S = max(1, sqrt(n)/16) apart around est (for two sets drawn from the same
-// distribution the index error is O(sqrt(n))); when the probes bracket the
-// key to at most 256 elements, one more round reads the bracket and counts
-// the elements below the key.  Otherwise round 2 probes the same way around
-// an interpolation of the key's value between B's first and last values
-// (loaded in round 1), and after that 129-ary rounds narrow what is left.
-__device__ __forceinline__ uint64_t warp_lower_bound_guess(const uint32_t *__restrict__ B,
-                                                           uint64_t n, const uint32_t *keyp,
-                                                           uint64_t est, uint32_t *key_out) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t key = __ldg(keyp);
-  const uint32_t bfirst = __ldg(B), blast = __ldg(B + n - 1);
-  uint64_t lo = 0, hi = n;  // answer in [lo, hi]
-  // 128 probes at positions p(k), k = 4*lane + j, clamped into [lo, hi)
-  auto narrow = [&](auto pos) {
-    uint64_t l = lo, h = hi;
-    uint64_t x[4];
-    uint32_t v[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      int64_t q = pos(4 * lane + j);
-      q = q < int64_t(lo) ? int64_t(lo) : q;
-      q = q > int64_t(hi) - 1 ? int64_t(hi) - 1 : q;
-      x[j] = uint64_t(q);
-      v[j] = __ldg(B + x[j]);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (v[j] < key) l = x[j] + 1 > l ? x[j] + 1 : l;
-      else h = x[j] < h ? x[j] : h;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const uint64_t l2 = __shfl_xor_sync(0xffffffffu, l, o);
-      const uint64_t h2 = __shfl_xor_sync(0xffffffffu, h, o);
-      l = l2 > l ? l2 : l;
-      h = h2 < h ? h2 : h;
-    }
-    lo = l;
-    hi = h;
-  };
-  if (n > 256) {
-    const int64_t S = int64_t(sqrtf(float(n)) * (1.0f / 16.0f)) > 1
-                          ? int64_t(sqrtf(float(n)) * (1.0f / 16.0f))
-                          : 1;
-    const int64_t g1 = int64_t(est < n ? est : n - 1);
-    narrow([&](int k) { return g1 + int64_t(k - 64) * S; });
-    if (hi - lo > 256) {
-      const uint64_t g2 =
-          (blast <= bfirst || key <= bfirst)
-              ? lo
-              : uint64_t(double(key - bfirst) / double(blast - bfirst) * double(n - 1));
-      const int64_t gg = int64_t(g2);
-      narrow([&](int k) { return gg + int64_t(k - 64) * S; });
-    }
-    while (hi - lo > 256) {
-      const uint64_t l0 = lo, span = hi - lo;
-      narrow([&](int k) { return int64_t(l0 + uint64_t(k + 1) * span / 129); });
-    }
-  }
-  // the bracket [lo, hi), at most 256 elements: count those below the key
-  uint32_t c = 0;
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const uint64_t i = lo + uint64_t(lane + 32 * j);
-    c += (i < hi && __ldg(B + i) < key) ? 1u : 0u;
-  }
-  *key_out = key;
-  return lo + __reduce_add_sync(0xffffffffu, c);
-}
-
-// A start index for reading B from the key *keyp on: some s <= the first index
-// i with B[i] >= key, at most S = max(1, sqrt(n)/8) below it -- for callers
-// that discard B elements below the key by value.  One round: the key and 64
-// probes S apart around the guess `est` are loaded together; the largest
-// probe below the key bounds s from below when some probe is not below it.
-// Otherwise (the guess was far off) the exact index, by
-// warp_lower_bound_guess.  All lanes take part and get the result.
-__device__ __forceinline__ uint64_t warp_start_below(const uint32_t *__restrict__ B, uint64_t n,
-                                                     const uint32_t *keyp, uint64_t est) {
-  const int lane = threadIdx.x & 31;
-  if (n <= 64) return 0;
-  const uint32_t key = __ldg(keyp);
-  const float r = sqrtf(float(n)) * 0.125f;
-  const int64_t S = r > 1.0f ? int64_t(r) : 1;
-  const int64_t g = int64_t(est < n ? est : n - 1);
-  uint64_t below = 0;  // largest probe below the key, + 1 (0: none)
-  bool above = false;  // some probe at or above the key
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    int64_t q = g + int64_t(2 * lane + j - 32) * S;
-    q = q < 0 ? 0 : (q > int64_t(n) - 1 ? int64_t(n) - 1 : q);
-    if (__ldg(B + q) < key) below = uint64_t(q) + 1 > below ? uint64_t(q) + 1 : below;
-    else above = true;
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const uint64_t b2 = __shfl_xor_sync(0xffffffffu, below, o);
-    below = b2 > below ? b2 : below;
-  }
-  // bracketed: below <= answer <= below - 1 + S (the next probe is not below)
-  if (__any_sync(0xffffffffu, above) && (below > 0 || g - 32 * S <= 0)) return below;
-  uint32_t k;
-  return warp_lower_bound_guess(B, n, keyp, est, &k);
-}
-
 // [v0, v1): the part of [lo, hi) of u32 array `base` whose elements can be
 // read with 16-byte loads (v0 the first index with a 16-byte aligned
 // address, v1 the last such boundary); v0 == v1 when there is none.

@@ -59,7 +59,9 @@ struct WWindowCfg {
   static constexpr uint32_t kSpan = uint32_t(VWW) * 32u;  // values per dense tile
   static constexpr int kRegion = VWW + 8;  // words per warp: dense probes reach word VWW
   static constexpr size_t kSmemBytes = size_t(kWarps) * kRegion * 4;
-  static constexpr int kTile = 4 * kTileWords * kWarps;  // A elements per CTA round
+  // grid sizing unit: a run of at least 32 A elements per warp (every warp
+  // streams its own B range, so a skewed pair still spreads over the GPU)
+  static constexpr int kTile = 32 * kWarps;
 };
 
 // Word q of X (n elements; element i is component (mis + i) & 3 of 16-byte
