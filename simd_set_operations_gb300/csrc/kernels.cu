@@ -29,11 +29,12 @@ KernelInfo mk_gallop(const char *name) {
                     NT, 0, GallopCfg<NT, GS, ITEMS, NSAMP>::kTile, name, MAT};
 }
 
-template <int NT, int UA, int UB, int VW, int MINB, bool MAT>
+template <int NT, int UA, int UB, int VW, int MINB, bool MAT, bool COARSE = false>
 KernelInfo mk_window(const char *name) {
-  using Cfg = WindowCfg<NT, UA, UB, VW, MAT>;
-  return KernelInfo{reinterpret_cast<const void *>(&window_kernel<NT, UA, UB, VW, MINB, MAT>), NT,
-                    Cfg::kSmemBytes, Cfg::kTile, name, MAT};
+  using Cfg = WindowCfg<NT, UA, UB, VW, MAT, COARSE>;
+  return KernelInfo{
+      reinterpret_cast<const void *>(&window_kernel<NT, UA, UB, VW, MINB, MAT, COARSE>), NT,
+      Cfg::kSmemBytes, Cfg::kTile, name, MAT};
 }
 
 template <int NT, int UA, int UB, int VWW, int MINB, bool MAT>
@@ -96,6 +97,9 @@ const KernelInfo kBitmapU32[][2] = {
     TILE_ROW(256, 4096, 4096, 8),    // 4: tile kernel (a B search per tile)
     WWINDOW_ROW(128, 4, 5, 512, 8),  // 5: warps on their own, 512-element tiles, 8 CTAs/SM
     WWINDOW_ROW(1024, 4, 5, 512, 1), // 6: the same, one CTA of 32 warps per SM
+    {mk_window<128, 4, 5, 2048, 8, false, true>("window_128_a4_b5_t2048_m8_coarse"),
+     mk_window<128, 4, 5, 2048, 8, true, true>("window_128_a4_b5_t2048_m8_coarse")},
+    // 7: variant 0 with coarse bitmaps for sparse tiles (size ratios 2-31)
 };
 
 // GS lanes per element (1 = thread per element with IT interleaved

@@ -28,6 +28,9 @@ struct KernelInfo {
 enum Algo { ALGO_MERGE = 1, ALGO_GALLOP = 2, ALGO_BITMAP = 3 };
 
 int num_variants(Algo algo, bool bsr);
+// SETOPS_ALGO_BITMAP variant with coarse bitmaps for sparse tiles (the
+// default for size ratios 2-31 and for SvS steps below the search ratio)
+constexpr int kCoarseBitmap = 7;
 // The fused k-set kernel (kset.cuh): count or materialise.
 const KernelInfo &kset_kernel(bool mat);
 constexpr int kKsetThreads = 128;

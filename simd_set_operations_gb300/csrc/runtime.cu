@@ -219,16 +219,20 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // arrays: ratio < 4: tiled bitmap; 4..31: merge-path; 32..511: sampled
+    // arrays: ratio < 2: tiled bitmap; 2..31: tiled bitmap with coarse
+    // bitmaps for sparse tiles (variant 7); 32..511: sampled
     // thread-per-element search; 512..8191: 8 lanes per element (4 elements
     // a warp); >= 8192: a warp per element.  BSR: merge-path below 32.
-    // (Measured on 2^10 / 2^14 / 2^18 x 2^24 pairs: each band's choice was
-    // the fastest variant there.)
+    // (Measured on 2^10 / 2^14 / 2^18 / 2^20-2^23 x 2^24 pairs: each band's
+    // choice was the fastest variant there.)
     unsigned v = (b < 5)    ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(0))
                  : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
                  : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3))
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
-    unsigned u = (b < 2) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(0)) : v, s = v;
+    unsigned u = (b < 1)   ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(0))
+                 : (b < 5) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kCoarseBitmap))
+                           : v,
+             s = v;
     ctx->policy[0][b] = u;
     ctx->policy[1][b] = s;
   }
@@ -253,9 +257,10 @@ int ctx_launch_pair(setops_ctx *ctx, const PairJob &j) {
     grid = std::max<uint64_t>(1, std::min(full, (total + per - 1) / per));
     status_words = grid;
   } else if (j.choice.algo == ALGO_BITMAP) {
-    // persistent grid over tiles of the smaller set; per-tile counts, then
-    // per-CTA block totals
-    ntiles = (mn + k.tile - 1) / k.tile;
+    // persistent grid: a CTA per two tiles' worth of both inputs (a balanced
+    // pair: a CTA per tile of the smaller set; a skewed one spreads the
+    // longer set's stream over the whole GPU)
+    ntiles = (na_ub + nb_ub + 2 * uint64_t(k.tile) - 1) / (2 * uint64_t(k.tile));
     grid = std::max<uint64_t>(1, std::min(full, ntiles));
     status_words = std::max<uint64_t>(ntiles, 1);
   } else {
@@ -884,8 +889,8 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
       // kernels; each checks the actual length ratio and only one runs.
       j.ratio_thr = thr;
       j.skip_rule = 2;
-      j.choice.algo = ALGO_MERGE;
-      j.choice.variant = int((ctx->policy[0][0] & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+      j.choice.algo = ALGO_BITMAP;  // tiles, coarse bitmaps for sparse ones
+      j.choice.variant = kCoarseBitmap;
       RK(ctx_launch_pair(ctx, j));
       j.skip_rule = 1;
       j.choice.algo = ALGO_GALLOP;

@@ -12,13 +12,19 @@
 // elements of A, values [w, alast]):
 //
 //   1. every thread loads UA 16-byte words of the tile (all loads in flight
-//      at once) and sets their bits in bitmap T of the value range (dense:
-//      alast - w < 32*VW), or keeps them as a sorted table in shared memory
-//      (sparse);
+//      at once) and sets their bits in bitmap T: one bit per value when the
+//      tile's span alast - w is below 32*VW (dense); else (COARSE) one bit
+//      per 2^sh values for the least sh that fits, and the tile is also kept
+//      as a sorted table in a second shared-memory region (without COARSE
+//      the sorted tile takes T's place);
 //   2. B is read from the current position b in windows of 4*UB*NT elements
 //      (UB 16-byte loads per thread in flight): each element tests its bit in
 //      T (an element below w or above alast lands on a zero bit: the index is
-//      clamped onto a zero word) or binary-searches the sparse table.  The
+//      clamped onto a zero word).  In a dense tile a set bit is a match; in
+//      a COARSE sparse one it is a candidate (a few per cent of the elements,
+//      since T is at most 1/32 full), and each lane binary-searches the
+//      sorted table for its candidates one at a time (without COARSE every
+//      element of a sparse tile searches it).  The
 //      window is a guess -- the tile's B range is not searched for -- so the
 //      elements up to alast are counted: sorted, they are a prefix of the
 //      window, b moves past them, and when the whole window was used the
@@ -49,28 +55,34 @@
 
 namespace setops {
 
-template <int NT, int UA, int UB, int VW, bool MAT>
+// COARSE: a tile too wide for one bit per value gets one bit per 2^sh values
+// and a sorted copy in shared memory (a second region); otherwise the sorted
+// tile takes T's place and every B element searches it.
+template <int NT, int UA, int UB, int VW, bool MAT, bool COARSE = false>
 struct WindowCfg {
   static_assert(NT % 32 == 0 && NT >= 64, "whole warps");
   static_assert(UA >= 1 && UB >= 1, "loads per thread");
   static constexpr int kTile = 4 * UA * NT;    // A elements per tile (aligned body)
   static constexpr int kWindow = 4 * UB * NT;  // B elements per window (aligned body)
-  static_assert((VW & (VW - 1)) == 0 && VW >= kTile, "a sparse tile (+6 end elements) fits T");
+  static_assert((VW & (VW - 1)) == 0 && (COARSE || VW >= kTile),
+                "power-of-two bitmap; without COARSE a sparse tile (+6 end elements) fits T");
   static constexpr uint32_t kSpan = uint32_t(VW) * 32u;
   static constexpr int kTabWords = VW + 8;
+  static constexpr int kSortWords = COARSE ? kTile + 8 : 0;  // the sorted tile (+6 end elements)
   static_assert(UB * 4 <= 30, "a thread's window hits fit one mask word");
-  static constexpr size_t kSmemBytes = size_t(kTabWords) * 4;
+  static constexpr size_t kSmemBytes = size_t(kTabWords + kSortWords) * 4;
 };
 
-template <int NT, int UA, int UB, int VW, int MINB, bool MAT>
+template <int NT, int UA, int UB, int VW, int MINB, bool MAT, bool COARSE = false>
 __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
-  using Cfg = WindowCfg<NT, UA, UB, VW, MAT>;
+  using Cfg = WindowCfg<NT, UA, UB, VW, MAT, COARSE>;
   constexpr int NW = NT / 32;
   constexpr uint32_t SPAN = Cfg::kSpan;
   constexpr uint32_t TA = Cfg::kTile;
 
   extern __shared__ __align__(128) uint32_t smem[];
-  uint32_t *tab = smem;  // T (dense) or the sorted A tile (sparse)
+  uint32_t *tab = smem;  // T: one bit per 2^sh values of the tile
+  uint32_t *srt = COARSE ? smem + Cfg::kTabWords : smem;  // the sorted tile (sparse)
   __shared__ unsigned long long s_b0;
   __shared__ uint32_t s_le[3];      // B elements of a window up to alast (rotating)
   __shared__ uint32_t s_wt[3][NW];  // materialise: matches of each warp in a window
@@ -133,7 +145,12 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
     const uint32_t nt = uint32_t(e1 - e0);
     const uint32_t w = __ldg(A + e0), alast = __ldg(A + e1 - 1);
     const uint32_t span = alast - w;
+    // T holds one bit per 2^sh values: sh = 0 (exact) when the tile's span
+    // fits (dense), else (COARSE) the least shift that makes it fit; then a
+    // set bit is only a candidate, checked against the sorted tile
     const bool dense = span < SPAN;
+    const uint32_t sh = (COARSE && !dense) ? 32u - __clz(span / SPAN) : 0u;
+    const uint32_t ssp = span >> sh;  // T's last bit
     {
       const uint4 *ta = A4 + ((amis + body0) >> 2);  // the body's 16-byte words
       const uint32_t nq = uint32_t((body1 - body0) >> 2);
@@ -154,11 +171,11 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
       uint32_t xe = 0;
       if (is_h) xe = __ldg(A + e0 + t);
       else if (is_t) xe = __ldg(A + body1 + (t - 32));
-      if (dense) {
+      if (COARSE || dense) {
         // (sorted input: every offset is at most span; the clamp keeps T's
         // bounds)
         auto ins = [&](uint32_t x) {
-          const uint32_t o = min(x - w, span);
+          const uint32_t o = min((x - w) >> sh, ssp);
           atomicOr(&tab[o >> 5], 1u << (o & 31));
         };
         auto ins4 = [&](const uint4 &v) {
@@ -176,21 +193,22 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
             if (uint32_t(u * NT + t) < nq) ins4(va[u]);
         }
         if (is_h || is_t) ins(xe);
-      } else {
-        // sparse: the tile itself in T's words, in order
+      }
+      if (!dense) {
+        // the tile itself, in order
 #pragma unroll
         for (int u = 0; u < UA; ++u) {
           const uint32_t qq = uint32_t(u * NT + t);
           if (qq < nq) {  // (tile 0 may start up to three head elements in: 4-byte stores)
-            uint32_t *d = tab + nh + 4 * qq;
+            uint32_t *d = srt + nh + 4 * qq;
             d[0] = va[u].x;
             d[1] = va[u].y;
             d[2] = va[u].z;
             d[3] = va[u].w;
           }
         }
-        if (is_h) tab[t] = xe;
-        else if (is_t) tab[uint32_t(body1 - e0) + (t - 32)] = xe;
+        if (is_h) srt[t] = xe;
+        else if (is_t) srt[uint32_t(body1 - e0) + (t - 32)] = xe;
       }
     }
     __syncthreads();
@@ -213,22 +231,25 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
     // staging run: one bit-plane ballot scan of the lanes' match counts
     // places them within the warp, and the warps' totals (exchanged at the
     // window's barrier) place the warps.
-    auto probe_dense = [&](uint32_t x) -> uint32_t {
-      const uint32_t o = min(x - w, span + 1);
+    // T's bit for x (an element outside [w, alast] lands on a zero bit past
+    // T's last; with sh > 0 a set bit is a candidate)
+    auto probe = [&](uint32_t x) -> uint32_t {
+      const uint32_t o = min((x - w) >> sh, ssp + 1);
       return __funnelshift_r(tab[o >> 5], 0u, o) & 1u;
     };
-    auto probe_sparse = [&](uint32_t x) -> uint32_t {
+    // x in the sorted tile
+    auto in_tile = [&](uint32_t x) -> bool {
       uint32_t lo = 0, len = nt;
       while (len > 0) {
         const uint32_t hh = len >> 1;
-        if (tab[lo + hh] < x) {
+        if (srt[lo + hh] < x) {
           lo += hh + 1;
           len -= hh + 1;
         } else {
           len = hh;
         }
       }
-      return (lo < nt && tab[lo] == x) ? 1u : 0u;
+      return lo < nt && srt[lo] == x;
     };
     for (;;) {
       if (b >= nb) break;
@@ -251,7 +272,7 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
         return MAT ? uint32_t(lane * UB + u) : uint32_t(u * 32 + lane);
       };
       uint32_t le = 0;  // elements up to alast: head / tail one by one, words x4
-      uint32_t hm = 0;  // materialise: bit 4u + k = element k of round u matched; bit 30 = xe
+      uint32_t hm = 0;  // bit 4u + k = element k of round u matched; bit 30 = xe
       uint4 vb[UB];
       auto ld = [&](int u) { return MAT ? __ldg(wq + wi(u)) : __ldcs(wq + wi(u)); };
       if (full) {
@@ -268,26 +289,43 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
       uint32_t xe = 0;
       if (is_h) xe = __ldg(B + b + lane);
       else if (is_t) xe = __ldg(B + bodyend + lane);
-      auto run = [&](auto probe) {
+      auto run = [&](auto pr) {
 #pragma unroll
         for (int u = 0; u < UB; ++u) {
           if (full || wb0 + wi(u) < nq) {
             const uint4 v = vb[u];
-            const uint32_t h = probe(v.x) | (probe(v.y) << 1) | (probe(v.z) << 2) | (probe(v.w) << 3);
-            if (MAT) hm |= h << (4 * u);
-            else cnt += uint32_t(__popc(h));
+            hm |= (pr(v.x) | (pr(v.y) << 1) | (pr(v.z) << 2) | (pr(v.w) << 3)) << (4 * u);
             le += v.w <= alast ? 4u : 0u;
           }
         }
         if (is_h || is_t) {
-          const uint32_t h = probe(xe);
-          if (MAT) hm |= h << 30;
-          else cnt += h;
+          hm |= pr(xe) << 30;
           le += xe <= alast ? 1u : 0u;
         }
       };
-      if (dense) run(probe_dense);
-      else run(probe_sparse);
+      if (COARSE || dense) run(probe);
+      else run([&](uint32_t x) -> uint32_t { return in_tile(x) ? 1u : 0u; });
+      if (COARSE && !dense) {
+        // candidates, one at a time: the element of bit c (4u + k, or 30 for
+        // xe) by selects, then the sorted tile
+        uint32_t cand = hm, ok = 0;
+        while (cand) {
+          const uint32_t c = uint32_t(__ffs(cand)) - 1u;
+          cand &= cand - 1u;
+          uint32_t x = xe;
+#pragma unroll
+          for (int u = 0; u < UB; ++u) {
+            const uint32_t q = c - 4u * uint32_t(u);
+            x = q == 0u ? vb[u].x : x;
+            x = q == 1u ? vb[u].y : x;
+            x = q == 2u ? vb[u].z : x;
+            x = q == 3u ? vb[u].w : x;
+          }
+          if (in_tile(x)) ok |= 1u << c;
+        }
+        hm = ok;
+      }
+      if (!MAT) cnt += uint32_t(__popc(hm));
       // one barrier per window: slot wc%3 sums this window; the slot of two
       // windows on is cleared (its last readers passed this barrier)
       le = __reduce_add_sync(0xffffffffu, le);
@@ -355,9 +393,9 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
       if (b < we) break;  // an element above alast: the tile is done
     }
 
-    // ---- 3. clear T (dense: the words used; sparse: the tile) ----
+    // ---- 3. clear T (the words used; without COARSE a sparse tile's table) ----
     {
-      const uint32_t tw = dense ? (span >> 5) + 1 : nt;
+      const uint32_t tw = (COARSE || dense) ? (ssp >> 5) + 1 : nt;
       for (uint32_t i = uint32_t(t); i < tw; i += NT) tab[i] = 0;
     }
     __syncthreads();  // T clear before the next tile's insertion
