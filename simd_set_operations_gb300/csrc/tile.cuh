@@ -45,7 +45,14 @@ struct TileCfg {
   static_assert((VW & (VW - 1)) == 0 && VW % 4 == 0, "power-of-two table");
   static constexpr uint32_t kSpan = uint32_t(VW) * 32u;  // values per dense tile
   static constexpr int kTabWords = VW + 4;                // + zero pad word group
-  static constexpr int kMWords = MAT ? VW : 0;            // match bitmap
+  // match bitmap M (materialise), whose upper half doubles as the coarse
+  // bitmap C of a sparse tile (M then holds one bit per A position, at most
+  // TA bits); count mode: C alone
+  // (+ 4: a zero word past C's last, where probes beyond the tile land)
+  static constexpr int kMWords = MAT ? VW + 4 : VW / 2 + 4;
+  static constexpr int kCOff = MAT ? VW / 2 : 0;          // C's first word in M
+  static constexpr uint32_t kCSpan = uint32_t(VW / 2) * 32u;  // values per coarse bitmap
+  static_assert(!MAT || (TA + 6 + 31) / 32 <= VW / 2, "M's position bits stay below C");
   static constexpr size_t kSmemBytes = size_t(kTabWords + kMWords) * 4;
   static constexpr int kTile = TA;
 };
@@ -189,6 +196,7 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
   constexpr uint32_t SPAN = Cfg::kSpan;
   constexpr int NW = NT / 32;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t *cbits = mbits + Cfg::kCOff;  // C (sparse tiles)
   // B's first and last values guide the searches (uniformly spread values
   // land close to the guess)
   const uint32_t bfirst = (search && nb) ? __ldg(B) : 0u;
@@ -209,6 +217,9 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
     const uint32_t w = __ldg(A + i0), alast = __ldg(A + i1 - 1);
     const bool dense = alast - w < SPAN;
     const uint32_t span = alast - w;
+    // sparse: C holds one bit per 2^csh values (the least shift that fits)
+    const uint32_t csh = dense ? 0u : 32u - __clz(span / Cfg::kCSpan);
+    const uint32_t cssp = span >> csh;  // C's last bit
 
     // ---- 1. B range (search warps) and A tile (the other warps) ----
     if (warp < searchers) {
@@ -232,7 +243,12 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
           atomicOr(&tab[o >> 5], 1u << (o & 31));
         });
       } else {
-        stream_elems(A + i0, ntile, h, e, tt, ns, [&](uint32_t j, uint32_t x) { tab[j] = x; });
+        // the sorted tile in T; C: one bit per 2^csh values of it
+        stream_elems(A + i0, ntile, h, e, tt, ns, [&](uint32_t j, uint32_t x) {
+          tab[j] = x;
+          const uint32_t o = (x - w) >> csh;
+          atomicOr(&cbits[o >> 5], 1u << (o & 31));
+        });
       }
     }
     __syncthreads();
@@ -258,7 +274,15 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
           }
         });
       } else {
-        stream_elems(B + b0, nbt, h, e, uint32_t(t), uint32_t(NT), [&](uint32_t, uint32_t x) {
+        // C's bit first (a few per cent of the elements land on a set bit);
+        // candidates binary-search the sorted tile.  Each thread takes two
+        // 16-byte words per step and searches only its candidates, one at a
+        // time, so a warp runs a search per candidate, not per element.
+        auto cbit = [&](uint32_t x) -> uint32_t {
+          const uint32_t o = min((x - w) >> csh, cssp + 1);
+          return (cbits[o >> 5] >> (o & 31)) & 1u;
+        };
+        auto check = [&](uint32_t x) {
           uint32_t lo = 0, len = ntile;
           while (len > 0) {
             const uint32_t hh = len >> 1;
@@ -273,7 +297,32 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
             if (MAT) atomicOr(&mbits[lo >> 5], 1u << (lo & 31));
             else ++cnt;
           }
-        });
+        };
+        const uint32_t *src = B + b0;
+        for (uint32_t j = uint32_t(t); j < h; j += NT) {
+          const uint32_t x = __ldg(src + j);
+          if (cbit(x)) check(x);
+        }
+        for (uint32_t j = e + uint32_t(t); j < nbt; j += NT) {
+          const uint32_t x = __ldg(src + j);
+          if (cbit(x)) check(x);
+        }
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src + h);  // 16-byte aligned
+        const uint32_t n4 = (e - h) / 4;
+        for (uint32_t u0 = uint32_t(t); u0 < n4; u0 += 2 * NT) {
+          const bool two = u0 + NT < n4;
+          const uint4 xa = __ldcs(s4 + u0);
+          const uint4 xb = two ? __ldcs(s4 + u0 + NT) : xa;
+          uint32_t cm = cbit(xa.x) | (cbit(xa.y) << 1) | (cbit(xa.z) << 2) | (cbit(xa.w) << 3);
+          if (two) cm |= (cbit(xb.x) | (cbit(xb.y) << 1) | (cbit(xb.z) << 2) | (cbit(xb.w) << 3)) << 4;
+          while (cm) {
+            const uint32_t c = uint32_t(__ffs(cm)) - 1u;
+            cm &= cm - 1u;
+            const uint4 v = c < 4u ? xa : xb;
+            const uint32_t k = c & 3u;
+            check(k == 0u ? v.x : k == 1u ? v.y : k == 2u ? v.z : v.w);
+          }
+        }
       }
     }
     __syncthreads();
@@ -316,11 +365,14 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
       staged += tot;
       __syncthreads();  // sparse: the A tile was read above; warp sums reused
     }
-    // clear T for the next tile (dense: the words used; sparse: the tile)
+    // clear T for the next tile (dense: the words used; sparse: the tile,
+    // and C's words used)
     {
       const uint32_t tw = dense ? (span >> 5) + 1 : ntile;
       for (uint32_t i = 4u * uint32_t(t); i < tw; i += 4u * NT)
         *reinterpret_cast<uint4 *>(tab + i) = make_uint4(0, 0, 0, 0);
+      if (!dense)
+        for (uint32_t i = uint32_t(t); i <= (cssp >> 5); i += NT) cbits[i] = 0;
     }
     __syncthreads();  // T clear before the next tile's insertion
   }
