@@ -8,8 +8,9 @@
 // nothing intermediate leaves shared memory:
 //
 //   CTA c owns the run S0[c*n0/G, (c+1)*n0/G) of the smallest set S0 and, for
-//   every other set Sj, a cursor bj (first found by one warp search per set,
-//   the searches spread over the warps).  Per tile of the run (TA elements,
+//   every other set Sj, a cursor bj (first placed by one round of probes per
+//   set around a guess, at most sqrt(|Sj|)/8 elements before the first
+//   element >= the run's first value; the rounds spread over the warps).  Per tile of the run (TA elements,
 //   values [w, alast]):
 //     1. the tile sets bits in bitmap X (dense: one bit per value of
 //        [w, alast]) or is kept as a sorted table with a bitmap X of its
@@ -117,7 +118,9 @@ __global__ void __launch_bounds__(NT, MINB) kset_kernel(const KsetArgs p) {
         const uint64_t q0 = (bmis + est) >> 2, q1 = ((bmis + guess(klast)) >> 2) + 1;
         prefetch_words_l2(B4, q0 > 512 ? q0 - 512 : 0, q1 + 512, bmis ? 1 : 0, (bmis + nb) >> 2);
       }
-      const uint64_t r = warp_lower_bound(B, nb, key, est);
+      // at or a little below the first element >= the run's first value (the
+      // elements read early lie below every value of the run: no bit of X)
+      const uint64_t r = warp_start_below(B, nb, A + ca0, est);
       if (lane == 0) s_b[j] = r;
     }
   }

@@ -816,7 +816,11 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
     const KernelInfo &kk = kset_kernel(mat);
     int occ = 1;
     RK(ctx_occupancy(ctx, kk, &occ));
-    const uint64_t ntiles = (mn + kk.tile - 1) / kk.tile;
+    // a CTA per two tiles' worth of all the sets (not of the smallest alone:
+    // each CTA's chain of windows through the other sets stays short)
+    uint64_t total = 0;
+    for (size_t i = 0; i < k; ++i) total += lens[i];
+    const uint64_t ntiles = (total + 2 * uint64_t(kk.tile) - 1) / (2 * uint64_t(kk.tile));
     const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(uint64_t(occ) * ctx->sms, ntiles));
     RK(ctx_status_words(ctx, grid));
     KsetArgs a{};
