@@ -209,3 +209,28 @@ def test_visitor_api(ctx, orc):
     w = so.UnsafeWriter.with_capacity(min(a.size, b.size))
     so.gpu_auto(a, b, w)
     assert np.array_equal(w.into(), want)
+
+
+def test_default_policy_bands(ctx, orc):
+    """The default policy per floor(log2(max/min)) band: arrays take the
+    window kernel below ratio 2, its coarse-bitmap variant (7) for 2-31, then
+    the search kernel (sampled, 8-lane, warp per element); BSR pairs take the
+    merge path below 32.  Each band's choice gives the oracle's result on a
+    pair of that ratio."""
+    def algo_var(flags):
+        return flags & 0xFF00, (flags >> 16) & 0xFF  # (algorithm bits, variant)
+    want_arr = {0: (so.ALGO_BITMAP, 0), 1: (so.ALGO_BITMAP, 7), 4: (so.ALGO_BITMAP, 7),
+                5: (so.ALGO_GALLOP, 0), 8: (so.ALGO_GALLOP, 0), 9: (so.ALGO_GALLOP, 3),
+                12: (so.ALGO_GALLOP, 3), 13: (so.ALGO_GALLOP, 2), 20: (so.ALGO_GALLOP, 2)}
+    for band, (algo, var) in want_arr.items():
+        got = algo_var(ctx.get_policy(False, band))
+        assert got == (algo, var), (band, got)
+    for band in (0, 4):
+        assert algo_var(ctx.get_policy(True, band))[0] == so.ALGO_MERGE
+    rng = np.random.default_rng(21)
+    for ratio in (1, 2, 3, 5, 16, 31, 32, 600, 9000):
+        na = 2000 if ratio < 600 else 200
+        a, b = pair_with_overlap(rng, na, na * ratio, na // 5, 1 << 32)
+        want = orc.naive_merge(a, b)
+        out, n = so.intersect(a, b, ctx=ctx)
+        assert np.array_equal(out[:n], want), ratio
