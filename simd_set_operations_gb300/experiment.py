@@ -15,8 +15,10 @@ The reference's pieces and what stands in for them here:
   from this library's seeded generators (the reference's are unseeded);
 * the timer registry (benchmark/src/timer.rs:75-259): names -> algorithms.
   Registered here: the GPU algorithms, ``gpu_auto``, ``gpu_merge``,
-  ``gpu_galloping``, ``gpu_bitmap`` (2-set; on k-set data: smallest-first
-  SvS with that kernel), ``gpu_svs`` (k-set, automatic), ``gpu_bsr`` (BSR
+  ``gpu_galloping``, ``gpu_bitmap``, ``gpu_bitmap_coarse`` (the tiled bitmap
+  kernel with coarse bitmaps for sparse tiles) (2-set; on k-set data:
+  smallest-first SvS with that kernel), ``gpu_svs`` (k-set, automatic),
+  ``gpu_bsr`` (BSR
   2-set; encoding outside the timed region, as the reference's harness,
   benchmark/src/timer/harness.rs:121-122).  Names of the reference's CPU
   algorithms are reported as unknown, as the reference does for names it
@@ -256,19 +258,26 @@ def _bsr_timer(ctx, sets, count_only, warmup_s):
     return _timed(ctx, call, warmup_s)
 
 
+# SETOPS_ALGO_BITMAP variant with coarse bitmaps for sparse tiles
+BITMAP_COARSE_VARIANT = 7
+
+
 def _registry() -> dict[str, Timer]:
-    from . import ALGO_BITMAP, ALGO_GALLOP, ALGO_MERGE
+    from . import ALGO_BITMAP, ALGO_GALLOP, ALGO_MERGE, VARIANT
     return {
         "gpu_auto": Timer("gpu_auto", _pair_timer(None)),
         "gpu_merge": Timer("gpu_merge", _pair_timer(ALGO_MERGE)),
         "gpu_galloping": Timer("gpu_galloping", _pair_timer(ALGO_GALLOP)),
         "gpu_bitmap": Timer("gpu_bitmap", _pair_timer(ALGO_BITMAP)),
+        "gpu_bitmap_coarse": Timer("gpu_bitmap_coarse",
+                                   _pair_timer(ALGO_BITMAP | VARIANT(BITMAP_COARSE_VARIANT))),
         "gpu_svs": Timer("gpu_svs", _svs_timer(None)),
         "gpu_bsr": Timer("gpu_bsr", _bsr_timer),
     }
 
 
-TIMER_NAMES = ("gpu_auto", "gpu_merge", "gpu_galloping", "gpu_bitmap", "gpu_svs", "gpu_bsr")
+TIMER_NAMES = ("gpu_auto", "gpu_merge", "gpu_galloping", "gpu_bitmap", "gpu_bitmap_coarse",
+               "gpu_svs", "gpu_bsr")
 
 
 def timer(name: str) -> Timer | None:

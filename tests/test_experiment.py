@@ -133,7 +133,7 @@ def test_results_layout_with_a_stand_in_timer(small):
 def test_registered_timers_run(small, ctx):
     exp, root = small
     ex.generate(exp, root)
-    exp["algorithm_sets"]["two"] = list(ex.TIMER_NAMES[:4]) + ["gpu_bsr"]
+    exp["algorithm_sets"]["two"] = list(ex.TIMER_NAMES[:5]) + ["gpu_bsr"]
     res = ex.run(exp, root, ctx=ctx, warmup_s=0.0, log=lambda m: None)
     for d in res["datasets"].values():
         for name, runs in d["algos"].items():
