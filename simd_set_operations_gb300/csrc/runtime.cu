@@ -204,6 +204,13 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
            : (pa == SETOPS_ALGO_BITMAP && !bsr)     ? ALGO_BITMAP
                                                     : ALGO_MERGE;
   c.variant = int((pol & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+  // default balanced band, arrays of at most 2^22: the coarse-bitmap variant
+  // (the same time on dense pairs there, about half on sparse ones; above
+  // 2^22 its larger shared-memory footprint costs a few per cent on dense
+  // pairs)
+  if (!bsr && band == 0 && !(ctx->policy_user[0] & 1u) && c.algo == ALGO_BITMAP &&
+      c.variant == 0 && mn <= (uint64_t(1) << 22))
+    c.variant = kCoarseBitmap;
   return c;
 }
 
@@ -219,7 +226,8 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // arrays: ratio < 2: tiled bitmap; 2..31: tiled bitmap with coarse
+    // arrays: ratio < 2: tiled bitmap (ctx_choose takes variant 7 for pairs
+    // of at most 2^22 under this default); 2..31: tiled bitmap with coarse
     // bitmaps for sparse tiles (variant 7); 32..511: sampled
     // thread-per-element search; 512..8191: 8 lanes per element (4 elements
     // a warp); >= 8192: a warp per element.  BSR: merge-path below 32.
@@ -478,6 +486,7 @@ int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
   if (v >= num_variants(al, bsr != 0)) return SETOPS_ERR_INVALID;
   ctx->policy[bsr ? 1 : 0][ratio_band] =
       algo_flags & (SETOPS_ALGO_MASK | SETOPS_VARIANT_MASK);
+  ctx->policy_user[bsr ? 1 : 0] |= 1u << ratio_band;
   return SETOPS_OK;
 }
 

@@ -69,6 +69,7 @@ struct setops_ctx {
   uint64_t launches = 0;
   std::map<const void *, int> occ;
   unsigned policy[2][setops::kRatioBands] = {};
+  uint32_t policy_user[2] = {};  // bit b: band b was set by setops_gpu_set_policy
   int batch_variant = 0;             // batch kernel shape
   uint32_t batch_search_ratio = 16;  // batch pairs with max/min >= this: search path
 
