@@ -96,10 +96,31 @@ def sweep_seeds(rank: int) -> list[int]:
     return [SEED + 1000 * rank + k for k in range(len(SMALL_EXPS))]
 
 
-def make_sweep(rank: int):
-    from simd_set_operations_gb300 import datasets as ds
+def make_sweep(rank: int, ds=None):
+    if ds is None:
+        from simd_set_operations_gb300 import datasets as ds
     return [ds.gen_twoset(sd, DENSITY, SELECTIVITY, 1 << e, LARGE)
             for sd, e in zip(sweep_seeds(rank), SMALL_EXPS)]
+
+
+def cpu_datasets():
+    """The input generators for a CPU-only process: datasets.py loaded on its
+    own (not through the package, whose import maps the GPU library) and
+    bound to the oracle's library, which is built from the same generator
+    source and so makes the same inputs."""
+    import importlib.util
+
+    import oracle
+    name = "setops_cpu_datasets"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(
+        name, ROOT / "simd_set_operations_gb300" / "datasets.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    mod.use_library(oracle.lib())
+    return mod
 
 
 def max_over_ranks(x: float) -> float:
@@ -271,7 +292,7 @@ def run_reference(args):
     import oracle
     oracle.lib()
     cores = oracle.host_cores()
-    pairs = make_sweep(0)
+    pairs = make_sweep(0, cpu_datasets())
     # warmup: algorithm choice per pair (bounded)
     _, _, detail, _, _, _ = cpu_sweep_best(pairs, 1, min(args.cpu_sample_seconds, 6.0))
     best = [next(k for k, v in oracle.ALGO_NAMES.items() if v == d["best"]) for d in detail]

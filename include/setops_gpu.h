@@ -296,7 +296,11 @@ int setops_srv_stop(setops_srv *srv);
  * overlapped on the GPU would race, so the call holds a per-device lock and
  * returns only when its work is done.  The first call on a device sets up
  * the array's device address (and the kernel's attributes); make that first
- * call before any stream capture. */
+ * call before any stream capture.  That first call is also when the CUDA
+ * runtime loads the array and the kernel onto the device (device code is
+ * loaded on first use unless CUDA_MODULE_LOADING=EAGER), so it takes device
+ * memory once: make it, with tiny inputs if need be, while the GPU still has
+ * memory free.  Later calls allocate nothing. */
 #define SETOPS_NOALLOC_MAX_SMALL ((size_t)1 << 20)
 int setops_gpu_intersect_noalloc(const uint32_t *a, size_t na,
                                  const uint32_t *b, size_t nb, uint32_t *out,

@@ -39,11 +39,16 @@ ALGO_NAMES = {
 }
 
 
-def build(ref: bool = True) -> None:
-    """make liboracle.so (and, when possible, the reference's kernels)."""
+GEN_SRC = HERE.parent / "simd_set_operations_gb300" / "csrc" / "gen.cpp"
+
+
+def build(ref_root: str | None = None) -> None:
+    """make liboracle.so and, when `ref_root` (the reference tree) is given,
+    the reference's own kernels into _ref/."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+    if ref_root:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={ref_root}"],
+                       check=True)
 
 
 _lib = None
@@ -53,8 +58,9 @@ _ref = None
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "oracle.c").stat().st_mtime:
-            build(ref=False)
+        if not LIB.exists() or any(LIB.stat().st_mtime < p.stat().st_mtime
+                                   for p in (HERE / "oracle.c", GEN_SRC)):
+            build()
         L = C.CDLL(str(LIB))
         vp, sz = C.c_void_p, C.c_size_t
         for name in ("orc_naive_merge", "orc_branchless_merge", "orc_galloping",

@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes as C
 from pathlib import Path
 
+from .datasets import GEN_SIGNATURES
+
 LIB_PATH = Path(__file__).resolve().parent / "libsetops_gpu.so"
 
 OK = 0
@@ -96,24 +98,11 @@ SIGNATURES = [
     ("setops_srv_poll", C.c_int, [vp, u64p, vp, sz, szp, u64p]),
     ("setops_srv_stats", C.c_int, [vp, u64p, u64p, u64p, u64p]),
     ("setops_srv_stop", C.c_int, [vp]),
-    # setops_bench.h
-    ("setops_gen_twoset", C.c_int, [u64, C.c_double, C.c_double, sz, sz, vp, vp]),
-    ("setops_gen_kset_lens", C.c_int, [sz, C.c_double, sz, szp]),
-    ("setops_gen_kset", C.c_int, [u64, C.c_double, C.c_double, sz, C.c_double, sz, C.POINTER(vp)]),
-    ("setops_gen_batch_sizes", C.c_int, [u64, sz, sz, sz, vp, vp]),
-    ("setops_gen_batch_fill", C.c_int, [u64, sz, vp, vp, vp, vp, C.c_double, C.c_double,
-                                        C.c_double, C.c_double, vp, C.c_int]),
-    ("setops_gen_index_lens", C.c_int, [sz, sz, C.c_double, vp]),
-    ("setops_gen_index_fill", C.c_int, [u64, sz, vp, vp, u64, vp, C.c_int]),
-    ("setops_gen_queries", C.c_int, [u64, sz, sz, C.c_uint32, C.c_uint32, C.c_double, vp, vp]),
-    ("setops_gen_bsr_encode", C.c_int, [vp, sz, vp, vp, vp, vp, vp, vp]),
+    # setops_bench.h (the generators and datafile functions are listed in datasets.py)
     ("setops_srv_run_load", C.c_int, [vp, vp, vp, sz, sz, C.c_double, u64, vp, vp,
                                       C.POINTER(C.c_double)]),
-    ("setops_gen_sorted_sample", C.c_int, [u64, sz, u64, vp]),
-    ("setops_datafile_write", C.c_int, [C.c_char_p, C.POINTER(vp), vp, sz]),
-    ("setops_datafile_read_header", C.c_int, [C.c_char_p, u64p, vp, sz]),
-    ("setops_datafile_read_sets", C.c_int, [C.c_char_p, C.POINTER(vp)]),
 ]
+SIGNATURES += GEN_SIGNATURES
 
 
 def _bind() -> None:

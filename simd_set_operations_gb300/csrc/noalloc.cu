@@ -23,6 +23,13 @@
 // once per device, with that device current.  The first call on a device
 // does that set-up (together with the kernel's shared-memory attribute and
 // occupancy query); that first call should come before any stream capture.
+// The set-up is also when the CUDA runtime, which loads a library's device
+// code on first use by default, loads the array and the kernel onto the
+// device: the first call therefore does take device memory, once.  A caller
+// whose GPU will later be full makes that first call (tiny inputs will do)
+// while memory is still free, or runs with CUDA_MODULE_LOADING=EAGER so that
+// everything is loaded when the process starts.  A set-up that failed is
+// tried again on the next call.
 //
 // Every call on a device shares the array, and a call leaves its contents
 // behind.  Each call therefore first zeroes what the kernel needs zeroed
@@ -32,7 +39,6 @@
 // point prevents that within a process by holding a per-device lock for the
 // whole call and returning only after its work on the stream has finished.
 #include <cstdint>
-#include <functional>
 #include <mutex>
 
 #include <cuda_runtime.h>
@@ -55,9 +61,8 @@ constexpr int kMaxDevices = 64;
 constexpr int kVariant = 0;
 
 struct DeviceSetup {
-  std::once_flag once;
-  std::mutex lock;      // one call at a time on this device
-  cudaError_t rc = cudaSuccess;
+  std::mutex lock;      // one call at a time on this device; guards the set-up
+  bool ready = false;   // set only by a set-up that succeeded
   unsigned char *base = nullptr;  // device address of the scratch array
   int sms = 0;
   int occ = 0;
@@ -72,8 +77,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
 
-// Once per device, with that device current.
-void setup_device(int dev, DeviceSetup &s) {
+// Once per device, with that device current and s.lock held.  A set-up
+// that fails leaves s.ready false, so the next call tries again.
+cudaError_t setup_device(int dev, DeviceSetup &s) {
   void *p = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev);
@@ -84,8 +90,10 @@ void setup_device(int dev, DeviceSetup &s) {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s.occ, k.fn, k.nt, k.dyn_smem);
   if (e == cudaSuccess && s.occ < 1) e = cudaErrorInvalidConfiguration;
+  if (e != cudaSuccess) return e;
   s.base = static_cast<unsigned char *>(p);
-  s.rc = e;
+  s.ready = true;
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -106,9 +114,8 @@ extern "C" int setops_gpu_intersect_noalloc(const uint32_t *a, size_t na,
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return SETOPS_ERR_CUDA;
   DeviceSetup &s = g_setup[dev];
-  std::call_once(s.once, setup_device, dev, std::ref(s));
-  if (s.rc != cudaSuccess) return SETOPS_ERR_CUDA;
   std::lock_guard<std::mutex> guard(s.lock);
+  if (!s.ready && setup_device(dev, s) != cudaSuccess) return SETOPS_ERR_CUDA;
 
   const setops::KernelInfo &k = setops::variant(setops::ALGO_MERGE, false, true, kVariant);
   const uint64_t total = uint64_t(na) + uint64_t(nb);

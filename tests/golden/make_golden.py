@@ -17,11 +17,13 @@
    property-test generators (setops/tests/testlib/mod.rs:102-153).  Values
    stay below 2^31 because those kernels compare as signed int.
 
-Items 1-2 are fixed data; item 3 needs an x86 host with the reference tree.
+Items 1-2 are fixed data; item 3 needs an x86 host with the reference tree,
+named by the environment variable SETOPS_REF_ROOT.
 """
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -107,7 +109,7 @@ def skewed_pair(rng):
 def make_ref_kernels(path: Path) -> None:
     import oracle
 
-    oracle.build(ref=True)
+    oracle.build(ref_root=os.environ.get("SETOPS_REF_ROOT"))
     if oracle.ref_lib() is None:
         print("skip ref_kernels.npz: reference kernels unavailable on this host")
         return

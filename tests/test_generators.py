@@ -123,3 +123,19 @@ def test_bsr_encode_batch_matches_oracle(orc):
     ba, sa, bb, sb = e.pair(1)
     assert list(ba) == [0] and list(sa) == [1]
     assert list(bb) == [0, 1, 0x7FFFFFF] and list(sb) == [0x80000000, 1, 0x80000000]
+
+
+def test_oracle_copy_of_the_generators_makes_the_same_inputs():
+    """The timed CPU reference path generates its inputs with the oracle's
+    build of the generator source (so that it maps no GPU library); those
+    inputs must be the GPU path's."""
+    import bench
+    from simd_set_operations_gb300 import datasets as ds
+    cds = bench.cpu_datasets()
+    for args in ((7, 0.05, 0.01, 1 << 10, 1 << 16), (8, 0.1, 0.1, 5000, 5000)):
+        for x, y in zip(ds.gen_twoset(*args), cds.gen_twoset(*args)):
+            assert np.array_equal(x, y)
+    b1, b2 = ds.gen_batch(3, 50, 16, 1 << 10), cds.gen_batch(3, 50, 16, 1 << 10)
+    assert np.array_equal(b1.pool, b2.pool) and np.array_equal(b1.a_len, b2.a_len)
+    k1, k2 = ds.gen_kset(5, 0.2, 0.05, 1 << 12, 1.0, 3), cds.gen_kset(5, 0.2, 0.05, 1 << 12, 1.0, 3)
+    assert all(np.array_equal(x, y) for x, y in zip(k1, k2))
