@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--bsr-pairs", type=int, default=10000,
                    help="pairs of the BSR subset of the batch leg")
     p.add_argument("--no-kset", action="store_true", help="skip the k-set leg")
+    p.add_argument("--no-config0", action="store_true",
+                   help="skip the plain 2^20 x 2^20 pair leg")
     p.add_argument("--no-serve", action="store_true",
                    help="skip the serving leg (k-set queries against a resident index)")
     p.add_argument("--serve-rates", default="10000,50000,200000,1000000",
@@ -143,6 +145,19 @@ def job_value(world: int, pairs_per_step: int, steps: int, seconds: float) -> fl
 
 def algorithmic_bytes(ns: int, nl: int, nout: int) -> int:
     return 4 * (ns + nl) + 4 * nout
+
+
+def touched_bytes(ns: int, nl: int, nout: int) -> int:
+    """Estimated bytes a search-band pair really moves: the small set read,
+    the output written, and in the large set the 32-byte sectors its probes
+    touch.  A search for one small element narrows a gap of about nl/ns
+    elements; the levels whose probes are more than one sector (8 elements)
+    apart each touch a sector of their own, the last ones share one:
+    max(1, ceil(log2(nl/ns)) - 2) sectors per element, capped at the whole
+    large set."""
+    import math
+    per = max(1, math.ceil(math.log2(max(nl / max(ns, 1), 2))) - 2)
+    return 4 * ns + 4 * nout + min(32 * per * ns, 4 * nl)
 
 
 def workload_config(sel=None):
@@ -361,7 +376,172 @@ def read_traffic():
     return int(m.group(1)) if m else None
 
 
+CONFIG0_SEED = 20240620
+
+
+def cpu_best_single_pair(a, b, seconds: float) -> dict:
+    """The reference's CPU path on one pair: each baseline (shuffling, SIMD
+    galloping, bmiss) timed single-core for about seconds/3, best kept; and
+    all cores, which the reference can only use on separate pairs, timed on
+    one copy of the pair per thread."""
+    import oracle
+    cores = oracle.host_cores()
+    out = np.empty(min(a.size, b.size), np.uint32)
+    per = {}
+    for algo in (oracle.SHUFFLING_W8, oracle.SIMD_GALLOPING_W16, oracle.BMISS_W4):
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            oracle.run_pairs(algo, [(a, b)], 1, outs=[out])
+            reps += 1
+            el = time.perf_counter() - t0
+            if el > seconds / 3 or reps >= 200:
+                break
+        per[oracle.ALGO_NAMES[algo]] = el / reps
+    best_name = min(per, key=per.get)
+    best = next(k for k, v in oracle.ALGO_NAMES.items() if v == best_name)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.run_pairs(best, [(a, b)] * cores, cores)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > max(0.5, seconds / 4) or reps >= 50:
+            break
+    return {"single_core": {"value": 1.0 / per[best_name], "cores": 1, "seconds_per_pair":
+                            per[best_name], "best": best_name, "all": per},
+            "all_cores": {"value": cores * reps / el, "cores": cores,
+                          "sample": f"{cores} copies of the pair, one per thread, {reps} rounds"},
+            "arch": os.uname().machine}
+
+
+def config0_leg(ctx, stream, cpu_seconds: float, with_cpu: bool) -> dict:
+    """The plain 2-set configuration: |A| = |B| = 2^20, element space
+    2^20 / 0.1, selectivity 0.1 (the reference's gen_twoset shape,
+    benchmark/src/generators.rs:30-68).  Materialised and counted on resident
+    inputs (CUDA events over 50 back-to-back launches), end to end through
+    the host-pointer call with copies, and the CPU path beside it; the GPU
+    result must equal naive_merge."""
+    import ctypes as C
+
+    import torch
+
+    import oracle
+    from simd_set_operations_gb300 import _lib, datasets as ds
+    L = _lib.lib
+    n = 1 << 20
+    a, b = ds.gen_twoset(CONFIG0_SEED, 0.1, 0.1, n, n)
+    want = oracle.naive_merge(a, b)
+    # 24 copies of the pair (192 MiB, more than the 129 MB L2), launches
+    # rotating over them so that each launch reads its inputs from HBM
+    ncopy = 24
+    da = torch.from_numpy(a.view(np.int32)).cuda()
+    db = torch.from_numpy(b.view(np.int32)).cuda()
+    copies = [(da, db)] + [(da.clone(), db.clone()) for _ in range(ncopy - 1)]
+    outs = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(ncopy)]
+    ln = torch.zeros(2 * ncopy, dtype=torch.int64, device="cuda")
+    h = ctx.handle
+
+    def launch(i: int, mat: bool):
+        x, y = copies[i % ncopy]
+        rc = L.setops_gpu_intersect_async(h, x.data_ptr(), n, y.data_ptr(), n,
+                                          outs[i % ncopy].data_ptr() if mat else None, n,
+                                          ln.data_ptr() + 8 * (2 * (i % ncopy) + (0 if mat else 1)),
+                                          0)
+        if rc != 0:
+            ctx.check(rc)
+
+    res = {}
+    for mat in (True, False):
+        for i in range(ncopy):
+            launch(i, mat)
+        ts = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for i in range(2 * ncopy):
+                launch(i, mat)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / (2 * ncopy))
+        res["materialise" if mat else "count"] = min(ts), statistics.mean(ts)
+    ctx.synchronize()
+    lens_all = ln.cpu().numpy()
+    if not np.all(lens_all == want.size):
+        raise SystemExit("config 0: a copy's GPU result length differs from naive_merge")
+    got = outs[ncopy - 1][:want.size].cpu().numpy().view(np.uint32)
+    del copies, outs
+    if not np.array_equal(got, want):
+        raise SystemExit("config 0: GPU result differs from naive_merge")
+    # end to end: pinned host buffers through setops_gpu_intersect(..., HOST)
+    pa = torch.from_numpy(a.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    pb = torch.from_numpy(b.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    po = torch.empty(n, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    nout = C.c_size_t()
+
+    def e2e_call():
+        ctx.check(L.setops_gpu_intersect(h, pa.ctypes.data, n, pb.ctypes.data, n, po.ctypes.data,
+                                         n, C.byref(nout), _lib.HOST))
+    for _ in range(3):
+        e2e_call()
+    reps = 30
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e2e_call()
+    e_el = (time.perf_counter() - t0) / reps
+    if nout.value != want.size or not np.array_equal(po[:want.size], want):
+        raise SystemExit("config 0: host-pointer result differs from naive_merge")
+    peak, kind = read_peak()
+    alg = 4 * 2 * n + 4 * want.size
+    ms = res["materialise"][1]
+    line = {
+        "workload": "plain 2-set pair: |A| = |B| = 2^20, element space 2^20 / 0.1, selectivity "
+                    "0.1, u32, materialised sorted output; checked equal to naive_merge",
+        "seed": CONFIG0_SEED, "out": int(want.size),
+        "pairs_per_s": 1e3 / ms, "ms": ms, "ms_min": res["materialise"][0],
+        "count_ms": res["count"][1],
+        "algorithmic_bytes": alg, "GBps_algorithmic": alg / (ms / 1e3) / 1e9,
+        "frac_of_peak": alg / (ms / 1e3) / 1e9 / peak, "peak_source": f"{kind} (hbm_gbs)",
+        "l2": "launches rotate over 24 device copies of the pair (192 MiB > 129 MB L2)",
+        "e2e": {"pairs_per_s": 1.0 / e_el, "ms_per_pair": 1e3 * e_el,
+                "h2d_bytes_per_pair": 8 * n, "d2h_bytes_per_pair": 4 * int(want.size) + 8,
+                "api": "setops_gpu_intersect(..., SETOPS_HOST), pinned host buffers"},
+        "results_match_naive_merge": True,
+    }
+    if with_cpu:
+        cpu = cpu_best_single_pair(a, b, cpu_seconds)
+        line["cpu_baseline"] = {"value": cpu["single_core"]["value"], "unit": "pairs/s",
+                                "cores": 1, "kind": "port", **cpu}
+    return line
+
+
 BATCH_SEED = 20240611
+
+
+def cpu_pairs_baseline(pairs, cores: int, caps) -> dict:
+    """The reference's CPU path over a batch of pairs: each baseline
+    (shuffling, SIMD galloping, bmiss) over every pair on all cores (pairs
+    spread over threads), best kept; and single-core on a 2,000-pair sample,
+    scaled to pairs/s."""
+    import oracle
+    outs = [np.empty(max(int(c), 1), np.uint32) for c in caps]
+    algos = (oracle.SHUFFLING_W8, oracle.SIMD_GALLOPING_W16, oracle.BMISS_W4)
+    allc, single = {}, {}
+    ns = min(len(pairs), 2000)
+    for algo in algos:
+        oracle.run_pairs(algo, pairs[:ns], cores, outs=outs[:ns])  # warm-up
+        t0 = time.perf_counter()
+        oracle.run_pairs(algo, pairs, cores, outs=outs)
+        allc[oracle.ALGO_NAMES[algo]] = len(pairs) / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.run_pairs(algo, pairs[:ns], 1, outs=outs[:ns])
+        single[oracle.ALGO_NAMES[algo]] = ns / (time.perf_counter() - t0)
+    best = max(allc, key=allc.get)
+    return {"value": allc[best], "unit": "pairs/s", "cores": cores, "kind": "port",
+            "best": best, "all_cores": allc,
+            "single_core": {"value": max(single.values()), "cores": 1,
+                            "best": max(single, key=single.get), "all": single,
+                            "sample_pairs": ns},
+            "sample": f"all {len(pairs)} pairs per baseline on {cores} threads",
+            "arch": os.uname().machine}
 
 
 def batch_leg(ctx, stream, npairs: int) -> dict:
@@ -415,34 +595,43 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
     matches = int(lens.sum().item())
     alg = 4 * int(b.pool.size) + 4 * matches
     steady = steady_state(ctx, stream, L, pool, arrs, npairs, out, cap, doffs, lens)
-    # the plain path: one launch per pair (async C-ABI on device pointers)
-    ns = min(npairs, 3000)
-    out2 = torch.empty(max(int(caps[:ns].sum()), 1), dtype=torch.int32, device="cuda")
-    ln2 = torch.zeros(ns, dtype=torch.int64, device="cuda")
-    base, obase, lbase = pool.data_ptr(), out2.data_ptr(), ln2.data_ptr()
+    # the plain path: one launch per pair (async C-ABI on device pointers),
+    # looped in C over every pair of the batch
+    out2 = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    ln2 = torch.zeros(npairs, dtype=torch.int64, device="cuda")
+    secs = C.c_double()
 
     def per_pair():
-        for p in range(ns):
-            rc = L.setops_gpu_intersect_async(
-                ctx.handle, base + 4 * int(b.a_off[p]), int(b.a_len[p]),
-                base + 4 * int(b.b_off[p]), int(b.b_len[p]), obase + 4 * int(offs[p]),
-                int(caps[p]), lbase + 8 * p, 0)
-            if rc != 0:
-                ctx.check(rc)
-        ctx.check(L.setops_gpu_synchronize(ctx.handle))
+        ctx.check(L.setops_bench_pairs_one_by_one(
+            ctx.handle, pool.data_ptr(), b.a_off.ctypes.data, b.a_len.ctypes.data,
+            b.b_off.ctypes.data, b.b_len.ctypes.data, npairs, out2.data_ptr(),
+            offs.ctypes.data, ln2.data_ptr(), C.byref(secs)))
+        return secs.value
 
     per_pair()
+    t_pp = min(per_pair() for _ in range(2))
+    # exactness: every pair of the batch equals the per-pair path and the
+    # oracle's naive_merge
+    import oracle
+    cores = oracle.host_cores()
+    l1, l2 = lens.cpu().numpy(), ln2.cpu().numpy()
+    o1, o2 = out.cpu().numpy().view(np.uint32), out2.cpu().numpy().view(np.uint32)
+    pairs = [b.pair(p) for p in range(npairs)]
+    exp = np.zeros(max(cap, 1), np.uint32)
+    views = [exp[int(offs[p]):int(offs[p]) + max(int(caps[p]), 0)] for p in range(npairs)]
     t0 = time.perf_counter()
-    per_pair()
-    t_pp = time.perf_counter() - t0
-    # exactness: the sample's per-pair results equal the batch's
-    l1, l2 = lens[:ns].cpu().numpy(), ln2.cpu().numpy()
-    o1 = out[:int(caps[:ns].sum())].cpu().numpy()
-    o2 = out2.cpu().numpy()
-    for p in range(ns):
-        lo, n1 = int(offs[p]), int(l1[p])
-        if n1 != int(l2[p]) or not np.array_equal(o1[lo:lo + n1], o2[lo:lo + n1]):
-            raise SystemExit(f"batched result of pair {p} differs from the per-pair path")
+    wl = oracle.run_pairs(oracle.NAIVE_MERGE, pairs, cores,
+                          outs=[v if v.size else exp[:1] for v in views])
+    t_oracle = time.perf_counter() - t0
+    mask = np.zeros(max(cap, 1) + 1, np.int64)
+    np.add.at(mask, offs.astype(np.int64), 1)
+    np.add.at(mask, (offs + wl).astype(np.int64), -1)
+    mask = np.cumsum(mask)[:max(cap, 1)] > 0
+    if not (np.array_equal(l1, wl.astype(np.int64)) and np.array_equal(l2, l1)):
+        raise SystemExit("batch: result lengths differ from naive_merge or the per-pair path")
+    if not (np.array_equal(o1[mask], exp[mask]) and np.array_equal(o2[mask], exp[mask])):
+        raise SystemExit("batch: results differ from naive_merge or the per-pair path")
+    cpu = cpu_pairs_baseline(pairs, cores, caps)
     peak, _ = read_peak()
     return {
         "workload": f"{npairs} pairs, sizes log-uniform in [2^4, 2^16] per set, density "
@@ -452,10 +641,14 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
         "GBps_algorithmic": alg / t_batch / 1e9, "frac_of_peak": alg / t_batch / 1e9 / peak,
         "policy": {"variant": int(v.value), "search_ratio": int(r.value),
                    "tuned_on_pairs": nt},
-        "one_launch_per_pair": {"pairs_per_s": ns / t_pp, "sample_pairs": ns,
-                                "api": "setops_gpu_intersect_async per pair, device pointers"},
-        "speedup_vs_one_launch_per_pair": (npairs / t_batch) / (ns / t_pp),
+        "one_launch_per_pair": {"pairs_per_s": npairs / t_pp, "pairs": npairs,
+                                "api": "setops_gpu_intersect_async per pair on device pointers, "
+                                       "looped in C (setops_bench_pairs_one_by_one)"},
+        "speedup_vs_one_launch_per_pair": (npairs / t_batch) / (npairs / t_pp),
         "results_match_per_pair_path": True,
+        "results_match_naive_merge": f"all {npairs} pairs (oracle, {cores} threads, "
+                                     f"{t_oracle:.1f} s)",
+        "cpu_baseline": cpu,
         "steady_state": steady,
     }
 
@@ -561,32 +754,60 @@ def batch_bsr_leg(ctx, stream, npairs: int) -> dict:
     t_batch = sorted(ts)[len(ts) // 2]
     words_out = int(lens.sum().item())
     alg = 8 * (int(bb.a_len.sum()) + int(bb.b_len.sum())) + 8 * words_out
-    # the plain path: one BSR call per pair (device pointers)
-    ns = min(npairs, 2000)
+    # the plain path: one BSR call per pair (device pointers), looped in C
+    # over every pair
     hb, hs, hl = ob.cpu().numpy().view(np.uint32), os_.cpu().numpy().view(np.uint32), lens.cpu().numpy()
-    ob2 = torch.empty(max(int(caps[:ns].max()) if ns else 1, 1), dtype=torch.int32, device="cuda")
+    ob2 = torch.empty(cap, dtype=torch.int32, device="cuda")
     os2 = torch.empty_like(ob2)
-    n_out = C.c_size_t()
-    pb, ps = bases.data_ptr(), states.data_ptr()
+    hl2 = np.zeros(npairs, np.uint64)
+    secs = C.c_double()
 
-    def per_pair(check):
-        for p in range(ns):
-            a0, na, b0, nb = int(bb.a_off[p]), int(bb.a_len[p]), int(bb.b_off[p]), int(bb.b_len[p])
-            ctx.check(L.setops_gpu_intersect_bsr(
-                ctx.handle, pb + 4 * a0, ps + 4 * a0, na, pb + 4 * b0, ps + 4 * b0, nb,
-                ob2.data_ptr(), os2.data_ptr(), ob2.numel(), C.byref(n_out), 0))
-            if check:
-                m = int(n_out.value)
-                lo = int(offs[p])
-                if m != int(hl[p]) or not (
-                        np.array_equal(ob2[:m].cpu().numpy().view(np.uint32), hb[lo:lo + m]) and
-                        np.array_equal(os2[:m].cpu().numpy().view(np.uint32), hs[lo:lo + m])):
-                    raise SystemExit(f"batched BSR result of pair {p} differs from the per-pair path")
+    def per_pair():
+        ctx.check(L.setops_bench_bsr_pairs_one_by_one(
+            ctx.handle, bases.data_ptr(), states.data_ptr(), bb.a_off.ctypes.data,
+            bb.a_len.ctypes.data, bb.b_off.ctypes.data, bb.b_len.ctypes.data, npairs,
+            ob2.data_ptr(), os2.data_ptr(), offs.ctypes.data, hl2.ctypes.data, C.byref(secs)))
+        return secs.value
 
-    per_pair(True)
-    t0 = time.perf_counter()
-    per_pair(False)
-    t_pp = time.perf_counter() - t0
+    per_pair()
+    t_pp = min(per_pair() for _ in range(2))
+    # exactness: every pair equals the per-pair path and the oracle's
+    # branchless_merge_bsr
+    import oracle
+    cores = oracle.host_cores()
+    pairs = [bb.pair(p) for p in range(npairs)]
+    eb, es = np.zeros(cap, np.uint32), np.zeros(cap, np.uint32)
+    vo = [(eb[int(offs[p]):int(offs[p]) + max(int(caps[p]), 1)],
+           es[int(offs[p]):int(offs[p]) + max(int(caps[p]), 1)]) for p in range(npairs)]
+    eb_pad = np.zeros(1, np.uint32)
+    vo = [v if v[0].size else (eb_pad, eb_pad.copy()) for v in vo]
+    wl = oracle.run_bsr_pairs(pairs, cores, outs=vo)
+    mask = np.zeros(cap + 1, np.int64)
+    np.add.at(mask, offs.astype(np.int64), 1)
+    np.add.at(mask, (offs + wl).astype(np.int64), -1)
+    mask = np.cumsum(mask)[:cap] > 0
+    hb2, hs2 = ob2.cpu().numpy().view(np.uint32), os2.cpu().numpy().view(np.uint32)
+    if not (np.array_equal(hl.astype(np.uint64), wl) and np.array_equal(hl2, wl)):
+        raise SystemExit("BSR batch: result lengths differ from branchless_merge_bsr")
+    if not all(np.array_equal(x[mask], y[mask]) for x, y in
+               ((hb, eb), (hs, es), (hb2, eb), (hs2, es))):
+        raise SystemExit("BSR batch: results differ from branchless_merge_bsr")
+    allc, single = {}, {}
+    ns = min(npairs, 2000)
+    for algo, name in ((0, "branchless_merge_bsr"), (1, "galloping_bsr")):
+        oracle.run_bsr_pairs(pairs[:ns], cores, algo=algo)
+        t0 = time.perf_counter()
+        oracle.run_bsr_pairs(pairs, cores, algo=algo)
+        allc[name] = npairs / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.run_bsr_pairs(pairs[:ns], 1, algo=algo)
+        single[name] = ns / (time.perf_counter() - t0)
+    best = max(allc, key=allc.get)
+    cpu = {"value": allc[best], "unit": "pairs/s", "cores": cores, "kind": "port", "best": best,
+           "all_cores": allc, "single_core": {"value": max(single.values()), "cores": 1,
+                                              "all": single, "sample_pairs": ns},
+           "sample": f"all {npairs} BSR pairs per baseline on {cores} threads (count only)",
+           "arch": os.uname().machine}
     peak, _ = read_peak()
     return {
         "workload": f"{npairs} BSR pairs at density 0.5 (sizes log-uniform in [2^4, 2^16] "
@@ -595,17 +816,55 @@ def batch_bsr_leg(ctx, stream, npairs: int) -> dict:
         "pairs": npairs, "words_in": int(bb.a_len.sum()) + int(bb.b_len.sum()),
         "words_out": words_out, "ms": 1e3 * t_batch, "pairs_per_s": npairs / t_batch,
         "GBps_algorithmic": alg / t_batch / 1e9, "frac_of_peak": alg / t_batch / 1e9 / peak,
-        "one_call_per_pair": {"pairs_per_s": ns / t_pp, "sample_pairs": ns,
-                              "api": "setops_gpu_intersect_bsr per pair, device pointers"},
-        "speedup_vs_one_call_per_pair": (npairs / t_batch) / (ns / t_pp),
+        "one_call_per_pair": {"pairs_per_s": npairs / t_pp, "pairs": npairs,
+                              "api": "setops_gpu_intersect_bsr per pair on device pointers, "
+                                     "looped in C (setops_bench_bsr_pairs_one_by_one)"},
+        "speedup_vs_one_call_per_pair": (npairs / t_batch) / (npairs / t_pp),
         "results_match_per_pair_path": True,
+        "results_match_branchless_merge_bsr": f"all {npairs} pairs",
+        "cpu_baseline": cpu,
     }
 
 
 KSET_SEED = 20240618
 
 
-def kset_leg(ctx, stream, ks=(3, 5, 8)) -> dict:
+def cpu_kset_baseline(sets, nout: int) -> dict:
+    """The reference's CPU k-set path (svs_generic, smallest first) with each
+    baseline as its 2-set function: single-core best (timed for about a
+    second each), and all cores on one copy of the group per thread."""
+    import oracle
+    cores = oracle.host_cores()
+    outs = [np.empty(max(min(x.size for x in sets), 1), np.uint32)]
+    per = {}
+    for algo in (oracle.SHUFFLING_W8, oracle.SIMD_GALLOPING_W16, oracle.BMISS_W4):
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            c = oracle.run_svs_groups([sets], 1, outs=outs, algo=algo)
+            reps += 1
+            el = time.perf_counter() - t0
+            if el > 1.0 or reps >= 100:
+                break
+        if int(c[0]) != nout:
+            raise SystemExit("CPU k-set baseline disagrees with svs_generic")
+        per[oracle.ALGO_NAMES[algo]] = reps / el
+    best_name = max(per, key=per.get)
+    best = next(k for k, v in oracle.ALGO_NAMES.items() if v == best_name)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.run_svs_groups([sets] * cores, cores, algo=best)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > 1.0 or reps >= 50:
+            break
+    return {"value": cores * reps / el, "unit": "k-sets/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} copies of the k-set, one per thread, {reps} rounds",
+            "best": best_name,
+            "single_core": {"value": per[best_name], "cores": 1, "all": per},
+            "arch": os.uname().machine}
+
+
+def kset_leg(ctx, stream, ks=(3, 5, 8), with_cpu: bool = True) -> dict:
     """The reference's k-set configuration: k sorted sets with |S_1| = 2^22
     and Zipf sizes |S_i| = 2^22 / i (exponent 1.0, the reference's skewness
     factor 1000 in thousandths), element space
@@ -682,11 +941,17 @@ def kset_leg(ctx, stream, ks=(3, 5, 8)) -> dict:
         core = int(0.05 * min(int(x.size) for x in sets))
         if int(n_out.value) < core:
             raise SystemExit(f"k={k}: {n_out.value} results, below the {core}-element core")
+        import oracle
+        want = oracle.svs_generic(sets)
+        if not np.array_equal(out[:int(n_out.value)].cpu().numpy().view(np.uint32), want):
+            raise SystemExit(f"k={k}: GPU result differs from svs_generic")
+        cpu = cpu_kset_baseline(sets, want.size) if with_cpu else None
         rows.append({"k": k, "sizes": [int(x.size) for x in sets], "out": int(n_out.value),
                      "ms": 1e3 * t_dev, "kset_per_s": 1.0 / t_dev,
                      "GBps_algorithmic": alg / t_dev / 1e9, "frac_of_peak": alg / t_dev / 1e9 / peak,
                      "ms_per_synchronous_call": 1e3 * t, "ms_graph_replay": 1e3 * t_graph,
-                     "GBps_graph_replay": alg / t_graph / 1e9})
+                     "GBps_graph_replay": alg / t_graph / 1e9,
+                     "results_match_svs_generic": True, "cpu_baseline": cpu})
     return {"workload": "k-set SvS: k in {3, 5, 8}, |S_i| = 2^22 / i, density 0.2, core 5 % of "
                         "the smallest set, u32, materialised, smallest first; inputs resident",
             "api": "setops_gpu_svs_async back to back, device pointers (ms); setops_gpu_svs, "
@@ -697,7 +962,37 @@ def kset_leg(ctx, stream, ks=(3, 5, 8)) -> dict:
 SERVE_SEED = 20240612
 
 
-def serve_leg(ctx, rates) -> dict:
+def cpu_serve_baseline(idx, ids, ks, plain_counts) -> dict:
+    """The reference's CPU path answering the same query stream: svs_generic
+    per query with each baseline as its 2-set function, queries spread over
+    all cores (8,000 queries), and single-core on 500; the answers' lengths
+    must equal the GPU's plain path's."""
+    import oracle
+    cores = oracle.host_cores()
+    groups = [sorted((idx.list(int(i)) for i in ids[q][:ks[q]]), key=len)
+              for q in range(min(8000, ks.size))]
+    allc, single = {}, {}
+    for algo in (oracle.SHUFFLING_W8, oracle.SIMD_GALLOPING_W16, oracle.BMISS_W4):
+        t0 = time.perf_counter()
+        c = oracle.run_svs_groups(groups, cores, algo=algo)
+        allc[oracle.ALGO_NAMES[algo]] = len(groups) / (time.perf_counter() - t0)
+        n = min(plain_counts.size, c.size)
+        if not np.array_equal(c[:n], plain_counts[:n]):
+            raise SystemExit("serving: CPU answers' lengths differ from the GPU's")
+        t0 = time.perf_counter()
+        oracle.run_svs_groups(groups[:500], 1, algo=algo)
+        single[oracle.ALGO_NAMES[algo]] = 500 / (time.perf_counter() - t0)
+    best = max(allc, key=allc.get)
+    return {"value": allc[best], "unit": "queries/s", "cores": cores, "kind": "port",
+            "best": best, "all_cores": allc,
+            "single_core": {"value": max(single.values()), "cores": 1, "all": single,
+                            "sample_queries": 500},
+            "sample": f"the first {len(groups)} queries of the stream, spread over {cores} "
+                      "threads (closed loop: throughput, no arrival process)",
+            "arch": os.uname().machine}
+
+
+def serve_leg(ctx, rates, with_cpu: bool = True) -> dict:
     """Served k-set queries (the reference's serving configuration): a
     resident index of 1,000,000 posting lists with rank-size Zipf(1.1)
     lengths clipped to [1, 2^20] over 2^26 documents; queries of k ~ U{2..6}
@@ -736,30 +1031,69 @@ def serve_leg(ctx, rates) -> dict:
                 "batches": st1["batches"] - st0["batches"],
                 "mean_batch": (st1["queries"] - st0["queries"]) / max(st1["batches"] - st0["batches"], 1),
             })
-    # the plain path: one synchronous k-set call per query on device pointers
+    # the plain path: one synchronous k-set call per query on device
+    # pointers, looped in C
     pool = torch.from_numpy(idx.pool.view(np.int32)).cuda()
-    base = pool.data_ptr()
     dout = torch.empty(1 << 20, dtype=torch.int32, device="cuda")
-    n = C.c_size_t()
-    times = []
-    nplain = 500
-    for q in range(nplain + 20):
-        k = int(ks[q])
-        sets = (C.c_void_p * k)(*[base + 4 * int(idx.offs[i]) for i in ids[q][:k]])
-        lens = (C.c_size_t * k)(*[int(idx.lens[i]) for i in ids[q][:k]])
-        t0 = time.perf_counter()
-        ctx.check(L.setops_gpu_svs(ctx.handle, sets, lens, k, dout.data_ptr(), dout.numel(),
-                                   C.byref(n), 0))
-        if q >= 20:
-            times.append(time.perf_counter() - t0)
-    tt = np.array(times) * 1e3
+    nplain = 2000
+    lat = np.zeros(nplain, np.uint64)
+    cnt = np.zeros(nplain, np.uint64)
+    secs = C.c_double()
+
+    def plain(nq):
+        ctx.check(L.setops_bench_queries_one_by_one(
+            ctx.handle, pool.data_ptr(), idx.offs.ctypes.data, idx.lens.ctypes.data,
+            ids.ctypes.data, ks.ctypes.data, ids.shape[1], nq, dout.data_ptr(), dout.numel(),
+            lat.ctypes.data, cnt.ctypes.data, C.byref(secs)))
+        return secs.value
+    plain(50)
+    el = plain(nplain)
+    tt = lat.astype(np.float64) * 1e-6
     out["plain_one_call_per_query"] = {
-        "api": "setops_gpu_svs per query, device pointers, sequential", "queries": nplain,
-        "qps": nplain / (tt.sum() * 1e-3), "p50_ms": float(np.percentile(tt, 50)),
+        "api": "setops_gpu_svs per query on device pointers, sequential, looped in C "
+               "(setops_bench_queries_one_by_one)", "queries": nplain,
+        "qps": nplain / el, "p50_ms": float(np.percentile(tt, 50)),
         "p99_ms": float(np.percentile(tt, 99))}
+    if with_cpu:
+        out["cpu_baseline"] = cpu_serve_baseline(idx, ids, ks, cnt)
     best = max(r["achieved_qps"] for r in out["rates"])
     out["best_served_qps"] = best
     out["speedup_vs_plain"] = best / out["plain_one_call_per_query"]["qps"]
+    return out
+
+
+def summarize(roofline, e2e, cpu, config0, batch, kset, serve) -> dict:
+    """The figures of every leg in a few keys, placed early in the line."""
+    g = lambda d, *ks: None if d is None else (  # noqa: E731
+        g(d.get(ks[0]), *ks[1:]) if len(ks) > 1 else d.get(ks[0]))
+    r = lambda x, n=3: None if x is None else round(float(x), n)  # noqa: E731
+    out = {"headline_frac": r(g(roofline, "frac")),
+           "sweep_e2e_pairs_per_s": r(g(e2e, "value"), 1),
+           "sweep_cpu_pairs_per_s": r(g(cpu, "value"), 1)}
+    if config0:
+        out["config0"] = {"pairs_per_s": r(config0["pairs_per_s"], 1),
+                          "frac": r(config0["frac_of_peak"]),
+                          "e2e_pairs_per_s": r(g(config0, "e2e", "pairs_per_s"), 1),
+                          "cpu_pairs_per_s": r(g(config0, "cpu_baseline", "value"), 1)}
+    if batch:
+        out["batch"] = {"pairs_per_s": r(batch["pairs_per_s"], 0),
+                        "frac": r(batch["frac_of_peak"]),
+                        "x_one_launch_per_pair": r(batch["speedup_vs_one_launch_per_pair"], 1),
+                        "cpu_pairs_per_s": r(g(batch, "cpu_baseline", "value"), 0),
+                        "bsr_pairs_per_s": r(g(batch, "bsr_subset", "pairs_per_s"), 0),
+                        "bsr_frac": r(g(batch, "bsr_subset", "frac_of_peak")),
+                        "bsr_x_one_call_per_pair":
+                            r(g(batch, "bsr_subset", "speedup_vs_one_call_per_pair"), 1),
+                        "bsr_cpu_pairs_per_s": r(g(batch, "bsr_subset", "cpu_baseline", "value"), 0)}
+    if kset:
+        out["kset"] = [{"k": row["k"], "ms": r(row["ms"], 4), "frac": r(row["frac_of_peak"]),
+                        "cpu_per_s": r(g(row, "cpu_baseline", "value"), 2)}
+                       for row in kset["rows"]]
+    if serve:
+        out["serve"] = {"best_qps": r(serve["best_served_qps"], 0),
+                        "x_plain": r(serve["speedup_vs_plain"], 1),
+                        "p99_ms": {str(x["offered_qps"]): r(x["p99_ms"]) for x in serve["rates"]},
+                        "cpu_qps": r(g(serve, "cpu_baseline", "value"), 0)}
     return out
 
 
@@ -893,9 +1227,14 @@ def run_gb300(args):
     for (s, l), p in zip(pairs, per_pair):
         n = int(SELECTIVITY * s.size)
         ms = statistics.mean(p)
-        sweep.append({"small": int(s.size), "large": int(l.size), "out": n,
-                      "ms_back_to_back": ms, "ms_min": min(p),
-                      "GBps_algorithmic": algorithmic_bytes(s.size, l.size, n) / (ms / 1e3) / 1e9})
+        row = {"small": int(s.size), "large": int(l.size), "out": n,
+               "ms_back_to_back": ms, "ms_min": min(p),
+               "GBps_algorithmic": algorithmic_bytes(s.size, l.size, n) / (ms / 1e3) / 1e9}
+        if l.size >= 32 * s.size:  # search band: the sectors the probes touch
+            tb = touched_bytes(s.size, l.size, n)
+            row["touched_bytes_est"] = tb
+            row["GBps_touched_est"] = tb / (ms / 1e3) / 1e9
+        sweep.append(row)
 
     # e2e through the host-pointer C ABI
     e2e = None
@@ -956,26 +1295,33 @@ def run_gb300(args):
                "host_cores": cores, "arch": os.uname().machine,
                "results_match_gpu": True}
 
+    config0 = None
+    if rank == 0 and not args.no_config0:
+        config0 = config0_leg(ctx, stream, min(args.cpu_sample_seconds, 6.0),
+                              with_cpu=not args.no_cpu_baseline)
     batch = None
     if rank == 0 and not args.no_batch:
         batch = batch_leg(ctx, stream, args.batch_pairs)
         batch["bsr_subset"] = batch_bsr_leg(ctx, stream, args.bsr_pairs)
     kset = None
     if rank == 0 and not args.no_kset:
-        kset = kset_leg(ctx, stream)
+        kset = kset_leg(ctx, stream, with_cpu=not args.no_cpu_baseline)
     serve = None
     if rank == 0 and not args.no_serve:
-        serve = serve_leg(ctx, [int(x) for x in args.serve_rates.split(",")])
+        serve = serve_leg(ctx, [int(x) for x in args.serve_rates.split(",")],
+                          with_cpu=not args.no_cpu_baseline)
 
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": UNIT,
+        "summary": summarize(roofline, e2e, cpu, config0, batch, kset, serve),
+        "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded; reference generator shape)",
         "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "batch": batch, "kset": kset,
-        "serve": serve,
+        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "config0": config0,
+        "batch": batch, "kset": kset, "serve": serve,
         "timing": {"bracket_ms_total": wall_ms, "headline_ms_total": sum(head_times),
                    "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
                            "sync inside; one event pair per step around the headline "

@@ -81,11 +81,15 @@ int setops_gen_bsr_encode(const uint32_t *pool, size_t nsets, const uint64_t *of
 /* Open-loop load for a server: query q (ids row q of an nq x kstride array,
  * ks[q] ids) arrives at the q-th point of a Poisson process of rate
  * rate_qps; latency_ns[q] runs from that arrival to completion, counts[q]
- * (optional) is the answer's length.  Returns when every query is done. */
+ * (optional) is the answer's length, and answers (optional, nq x
+ * answer_stride u32) receives the answer itself in row q
+ * (SETOPS_ERR_CAPACITY when one is longer than answer_stride).  Returns when
+ * every query is done.  Exported by libsetops_gpu.so. */
 struct setops_srv;
 int setops_srv_run_load(struct setops_srv *srv, const uint32_t *ids, const uint32_t *ks,
                         size_t kstride, size_t nq, double rate_qps, uint64_t seed,
-                        uint64_t *latency_ns, uint64_t *counts, double *elapsed_s);
+                        uint64_t *latency_ns, uint64_t *counts, uint32_t *answers,
+                        size_t answer_stride, double *elapsed_s);
 
 /* Sorted, duplicate-free sample of n values from [0, max_value). */
 int setops_gen_sorted_sample(uint64_t seed, size_t n, uint64_t max_value,
@@ -105,6 +109,44 @@ int setops_datafile_write(const char *path, const uint32_t *const *sets,
 int setops_datafile_read_header(const char *path, uint64_t *set_count,
                                 uint64_t *lens, size_t max_sets);
 int setops_datafile_read_sets(const char *path, uint32_t *const *sets);
+
+/* The plain GPU paths a caller without batching or serving writes, looped
+ * in C so that their timing holds no foreign-language call overhead (they
+ * are the baselines of the batched and served paths).  Exported by
+ * libsetops_gpu.so; `ctx` is a setops_ctx.
+ *
+ * setops_bench_pairs_one_by_one: one setops_gpu_intersect_async launch per
+ * pair p, on device data: A = pool + a_off[p] (a_len[p] elements), B likewise,
+ * output at out + out_off[p] (capacity min(a_len[p], b_len[p])), length to
+ * the device word lens_dev[p]; then one setops_gpu_synchronize.  The offset
+ * and length arrays are host arrays.  *seconds: wall time of the loop and the
+ * synchronisation. */
+struct setops_ctx;
+int setops_bench_pairs_one_by_one(struct setops_ctx *ctx, const uint32_t *pool,
+                                  const uint64_t *a_off, const uint64_t *a_len,
+                                  const uint64_t *b_off, const uint64_t *b_len, size_t npairs,
+                                  uint32_t *out, const uint64_t *out_off, uint64_t *lens_dev,
+                                  double *seconds);
+/* The same for BSR pairs: one setops_gpu_intersect_bsr call (which returns
+ * the result length, so each call waits for its pair) per pair, words at
+ * bases/states + a_off[p] etc. on the device, the result of pair p at
+ * out_bases/out_states + out_off[p]; lens (host) gets each length. */
+int setops_bench_bsr_pairs_one_by_one(struct setops_ctx *ctx, const uint32_t *bases,
+                                      const uint32_t *states, const uint64_t *a_off,
+                                      const uint64_t *a_len, const uint64_t *b_off,
+                                      const uint64_t *b_len, size_t npairs, uint32_t *out_bases,
+                                      uint32_t *out_states, const uint64_t *out_off,
+                                      uint64_t *lens, double *seconds);
+/* One setops_gpu_svs call per query q, in order: lists ids[q * kstride +
+ * 0 .. ks[q]) of a device pool (list i = pool + offs[i], lens[i] elements;
+ * offs and lens are host arrays), the answer to the device buffer out
+ * (capacity out_cap, reused by every query).  latency_ns[q] (optional) gets
+ * the call's wall time and counts[q] (optional) its answer's length. */
+int setops_bench_queries_one_by_one(struct setops_ctx *ctx, const uint32_t *pool,
+                                    const uint64_t *offs, const uint64_t *lens,
+                                    const uint32_t *ids, const uint32_t *ks, size_t kstride,
+                                    size_t nq, uint32_t *out, size_t out_cap,
+                                    uint64_t *latency_ns, uint64_t *counts, double *seconds);
 
 #ifdef __cplusplus
 }

@@ -88,6 +88,20 @@ const char *setops_status_string(int status);
 int setops_gpu_num_variants(unsigned algo, int bsr);
 /* Number of kernels this context has launched (for launch accounting). */
 uint64_t setops_gpu_launch_count(const setops_ctx *ctx);
+
+/* Bounded device waits (no counterpart: the reference runs on the CPU and
+ * never waits on a GPU).  Every spin-wait in this library's kernels (a bulk
+ * copy's barrier, a predecessor's published count, a grid-wide flag) gives
+ * up after a time limit, records the fact and returns, so that the call
+ * fails with SETOPS_ERR_TIMEOUT instead of hanging the GPU; the context
+ * stays usable.  setops_gpu_set_wait_limit_ns sets that limit in
+ * nanoseconds (0 = the default, 2 s) for every context on ctx's device; call
+ * it while no work of this library runs on that device.
+ * setops_gpu_check_wait_limit runs one wait that nothing ever satisfies and
+ * returns SETOPS_ERR_TIMEOUT when the limit ended it, with *waited_ns the
+ * time the device waited. */
+int setops_gpu_set_wait_limit_ns(setops_ctx *ctx, uint64_t ns);
+int setops_gpu_check_wait_limit(setops_ctx *ctx, uint64_t *waited_ns);
 /* Algorithm policy: the kernel used for pairs whose size ratio max/min lies
  * in [2^band, 2^(band+1)), band in [0, 32); algo_flags = SETOPS_ALGO_MERGE,
  * SETOPS_ALGO_GALLOP or SETOPS_ALGO_BITMAP (arrays only) | SETOPS_VARIANT(v).

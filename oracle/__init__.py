@@ -90,6 +90,14 @@ def lib() -> C.CDLL:
         L.orc_run_svs_groups.argtypes = [sz, C.POINTER(vp), C.POINTER(sz),
                                          C.POINTER(sz), C.POINTER(vp),
                                          C.POINTER(C.c_uint64), C.c_int]
+        L.orc_run_bsr_pairs.restype = C.c_int
+        L.orc_run_bsr_pairs.argtypes = [C.c_int, sz] + [C.POINTER(vp)] * 2 + [C.POINTER(sz)] + \
+            [C.POINTER(vp)] * 2 + [C.POINTER(sz)] + [C.POINTER(vp)] * 2 + \
+            [C.POINTER(C.c_uint64), C.c_int]
+        L.orc_run_svs_groups_algo.restype = C.c_int
+        L.orc_run_svs_groups_algo.argtypes = [C.c_int, sz, C.POINTER(vp), C.POINTER(sz),
+                                              C.POINTER(sz), C.POINTER(vp),
+                                              C.POINTER(C.c_uint64), C.c_int]
         _lib = L
     return _lib
 
@@ -225,8 +233,9 @@ def run_pairs(algo: int, pairs, nthreads: int = 1, outs=None) -> np.ndarray:
     return counts
 
 
-def run_svs_groups(groups, nthreads: int = 1, outs=None) -> np.ndarray:
-    """k-set groups [[s0, s1, ...], ...] through svs_generic(naive_merge)."""
+def run_svs_groups(groups, nthreads: int = 1, outs=None, algo: int = NAIVE_MERGE) -> np.ndarray:
+    """k-set groups [[s0, s1, ...], ...] through svs_generic with the 2-set
+    function `algo` in every step (naive_merge by default)."""
     flat = [_u32(s) for g in groups for s in g]
     offs = np.zeros(len(groups) + 1, np.uintp)
     offs[1:] = np.cumsum([len(g) for g in groups])
@@ -236,11 +245,30 @@ def run_svs_groups(groups, nthreads: int = 1, outs=None) -> np.ndarray:
     OF = (C.c_size_t * (len(groups) + 1))(*[int(x) for x in offs])
     O = (C.c_void_p * len(groups))(*[o.ctypes.data for o in outs]) if outs is not None else None
     counts = np.zeros(len(groups), np.uint64)
-    rc = lib().orc_run_svs_groups(len(groups), S, L, OF, O,
-                                  counts.ctypes.data_as(C.POINTER(C.c_uint64)), nthreads)
+    rc = lib().orc_run_svs_groups_algo(algo, len(groups), S, L, OF, O,
+                                       counts.ctypes.data_as(C.POINTER(C.c_uint64)), nthreads)
     if rc != 0:
-        raise ValueError("orc_run_svs_groups: bad argument")
+        raise ValueError("orc_run_svs_groups_algo: bad argument")
     return counts
+
+
+def run_bsr_pairs(pairs, nthreads: int = 1, outs=None, algo: int = 0) -> np.ndarray:
+    """BSR pairs [(ba, sa, bb, sb), ...] through branchless_merge_bsr (algo
+    0) or galloping_bsr (1) on `nthreads` threads; returns word counts.
+    `outs` ([(out_bases, out_states), ...]) materialises."""
+    n = len(pairs)
+    keep = [tuple(_u32(x) for x in p) for p in pairs]
+    P = lambda j: (C.c_void_p * n)(*[_ptr(p[j]) for p in keep])  # noqa: E731
+    NA = (C.c_size_t * n)(*[p[0].size for p in keep])
+    NB = (C.c_size_t * n)(*[p[2].size for p in keep])
+    OB = (C.c_void_p * n)(*[o[0].ctypes.data for o in outs]) if outs is not None else None
+    OS = (C.c_void_p * n)(*[o[1].ctypes.data for o in outs]) if outs is not None else None
+    words = np.zeros(n, np.uint64)
+    rc = lib().orc_run_bsr_pairs(algo, n, P(0), P(1), NA, P(2), P(3), NB, OB, OS,
+                                 words.ctypes.data_as(C.POINTER(C.c_uint64)), nthreads)
+    if rc != 0:
+        raise ValueError("orc_run_bsr_pairs: bad argument")
+    return words
 
 
 # ---- the reference's own C++ kernels (x86 only) ---------------------------

@@ -222,22 +222,33 @@ size_t orc_galloping_bsr(const uint32_t *ba, const uint32_t *sa, size_t na,
 /* svs_generic (setops/src/intersect/svs.rs:50-73) with naive_merge: the
  * first two sets go to `left`; every further set swaps the two buffers and
  * intersects the previous result (now in `right`) with it into `left`. */
-size_t orc_svs_generic(const uint32_t *const *sets, const size_t *lens,
+typedef size_t (*pair_fn)(const uint32_t *, size_t, const uint32_t *, size_t,
+                          uint32_t *);
+
+/* svs_generic with the 2-set function `f` (the reference passes f as a
+ * parameter, svs.rs:50). */
+static size_t svs_with(pair_fn f, const uint32_t *const *sets, const size_t *lens,
                        size_t k, uint32_t *left, uint32_t *right,
                        uint32_t **result) {
   if (k < 2) {
     if (result) *result = left;
     return 0;
   }
-  size_t n = orc_naive_merge(sets[0], lens[0], sets[1], lens[1], left);
+  size_t n = f(sets[0], lens[0], sets[1], lens[1], left);
   for (size_t s = 2; s < k; s++) {
     uint32_t *t = left;
     left = right;
     right = t;
-    n = orc_naive_merge(right, n, sets[s], lens[s], left);
+    n = f(right, n, sets[s], lens[s], left);
   }
   if (result) *result = left;
   return n;
+}
+
+size_t orc_svs_generic(const uint32_t *const *sets, const size_t *lens,
+                       size_t k, uint32_t *left, uint32_t *right,
+                       uint32_t **result) {
+  return svs_with(orc_naive_merge, sets, lens, k, left, right, result);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -428,9 +439,6 @@ size_t orc_bmiss_w4(const uint32_t *a, size_t na, const uint32_t *b,
 /* Multi-pair runner: pairs spread over threads (the reference itself is
  * single-threaded; this is the all-cores CPU baseline harness). */
 
-typedef size_t (*pair_fn)(const uint32_t *, size_t, const uint32_t *, size_t,
-                          uint32_t *);
-
 static pair_fn algo_fn(int algo) {
   switch (algo) {
     case ORC_NAIVE_MERGE: return orc_naive_merge;
@@ -495,8 +503,8 @@ static void *svs_worker(void *arg) {
       continue;
     }
     uint32_t *res = NULL;
-    size_t c = orc_svs_generic(J->sets + o, J->lens + o, k, buf, buf + cap + 1,
-                               &res);
+    size_t c = svs_with(J->fn ? J->fn : orc_naive_merge, J->sets + o, J->lens + o, k, buf,
+                        buf + cap + 1, &res);
     if (J->outs && J->outs[g]) memcpy(J->outs[g], res, c * sizeof(uint32_t));
     J->counts[g] = c;
     free(buf);
@@ -545,9 +553,19 @@ int orc_run_pairs(int algo, size_t n, const uint32_t *const *as,
 int orc_run_svs_groups(size_t ngroups, const uint32_t *const *sets,
                        const size_t *lens, const size_t *offs,
                        uint32_t *const *outs, uint64_t *counts, int nthreads) {
+  return orc_run_svs_groups_algo(ORC_NAIVE_MERGE, ngroups, sets, lens, offs, outs, counts,
+                                 nthreads);
+}
+
+int orc_run_svs_groups_algo(int algo, size_t ngroups, const uint32_t *const *sets,
+                            const size_t *lens, const size_t *offs,
+                            uint32_t *const *outs, uint64_t *counts, int nthreads) {
+  pair_fn fn = algo_fn(algo);
+  if (!fn || fn == orc_galloping) return -1; /* galloping needs the smaller set first */
   if (ngroups && (!sets || !lens || !offs || !counts)) return -1;
   job_t J;
   memset(&J, 0, sizeof J);
+  J.fn = fn;
   J.n = ngroups;
   J.sets = sets;
   J.lens = lens;
@@ -555,4 +573,71 @@ int orc_run_svs_groups(size_t ngroups, const uint32_t *const *sets,
   J.outs = outs;
   J.counts = counts;
   return run_threads(&J, svs_worker, nthreads);
+}
+
+/* BSR pairs spread over threads: pair i = (ba[i], sa[i], na[i]) x (bb[i],
+ * sb[i], nb[i]) through branchless_merge_bsr (algo 0) or galloping_bsr
+ * (algo 1, the first set taken as the smaller); words[i] gets the result's
+ * word count, results to ob[i]/os[i] when given. */
+typedef size_t (*bsr_fn)(const uint32_t *, const uint32_t *, size_t, const uint32_t *,
+                         const uint32_t *, size_t, uint32_t *, uint32_t *, uint64_t *);
+
+typedef struct {
+  bsr_fn fn;
+  size_t n;
+  const uint32_t *const *ba, *const *sa, *const *bb, *const *sb;
+  const size_t *na, *nb;
+  uint32_t *const *ob, *const *os;
+  uint64_t *words;
+  atomic_size_t next;
+} bsr_job_t;
+
+static void *bsr_worker(void *arg) {
+  bsr_job_t *J = (bsr_job_t *)arg;
+  for (;;) {
+    size_t i = atomic_fetch_add(&J->next, 1);
+    if (i >= J->n) break;
+    J->words[i] = J->fn(J->ba[i], J->sa[i], J->na[i], J->bb[i], J->sb[i], J->nb[i],
+                        J->ob ? J->ob[i] : NULL, J->os ? J->os[i] : NULL, NULL);
+  }
+  return NULL;
+}
+
+int orc_run_bsr_pairs(int algo, size_t n, const uint32_t *const *ba,
+                      const uint32_t *const *sa, const size_t *na,
+                      const uint32_t *const *bb, const uint32_t *const *sb,
+                      const size_t *nb, uint32_t *const *ob, uint32_t *const *os,
+                      uint64_t *words, int nthreads) {
+  if ((algo != 0 && algo != 1) || (n && (!ba || !sa || !na || !bb || !sb || !nb || !words)))
+    return -1;
+  if ((ob == NULL) != (os == NULL)) return -1;
+  bsr_job_t J;
+  memset(&J, 0, sizeof J);
+  J.fn = algo == 0 ? orc_branchless_merge_bsr : orc_galloping_bsr;
+  J.n = n;
+  J.ba = ba;
+  J.sa = sa;
+  J.na = na;
+  J.bb = bb;
+  J.sb = sb;
+  J.nb = nb;
+  J.ob = ob;
+  J.os = os;
+  J.words = words;
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 512) nthreads = 512;
+  atomic_store(&J.next, 0);
+  if (nthreads == 1) {
+    bsr_worker(&J);
+    return 0;
+  }
+  pthread_t th[512];
+  int started = 0;
+  for (int t = 0; t < nthreads; t++) {
+    if (pthread_create(&th[t], NULL, bsr_worker, &J) != 0) break;
+    started++;
+  }
+  if (started == 0) bsr_worker(&J);
+  for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+  return 0;
 }

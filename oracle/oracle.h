@@ -144,6 +144,20 @@ int orc_run_pairs(int algo, size_t n, const uint32_t *const *as,
 int orc_run_svs_groups(size_t ngroups, const uint32_t *const *sets,
                        const size_t *lens, const size_t *offs,
                        uint32_t *const *outs, uint64_t *counts, int nthreads);
+/* The same with the 2-set function `algo` (an ORC_* id other than
+ * ORC_GALLOPING) in every SvS step, as svs_generic takes it as a parameter
+ * (setops/src/intersect/svs.rs:50): the timed CPU baseline of k-set work. */
+int orc_run_svs_groups_algo(int algo, size_t ngroups, const uint32_t *const *sets,
+                            const size_t *lens, const size_t *offs,
+                            uint32_t *const *outs, uint64_t *counts, int nthreads);
+
+/* BSR pairs over threads: branchless_merge_bsr (algo 0) or galloping_bsr
+ * (algo 1) per pair; words[i] = result word count; ob/os optional. */
+int orc_run_bsr_pairs(int algo, size_t n, const uint32_t *const *ba,
+                      const uint32_t *const *sa, const size_t *na,
+                      const uint32_t *const *bb, const uint32_t *const *sb,
+                      const size_t *nb, uint32_t *const *ob, uint32_t *const *os,
+                      uint64_t *words, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -97,6 +97,18 @@ class Context:
     def launch_count(self) -> int:
         return int(lib.setops_gpu_launch_count(self.handle))
 
+    def set_wait_limit_ns(self, ns: int) -> None:
+        """Time limit of the kernels' bounded device waits on this context's
+        device (0 = the default, 2 s)."""
+        self.check(lib.setops_gpu_set_wait_limit_ns(self.handle, int(ns)))
+
+    def check_wait_limit(self) -> tuple[int, int]:
+        """Runs one device wait that nothing satisfies; returns (status,
+        waited_ns): SETOPS_ERR_TIMEOUT once the limit ended the wait."""
+        w = C.c_uint64()
+        rc = lib.setops_gpu_check_wait_limit(self.handle, C.byref(w))
+        return int(rc), int(w.value)
+
     def set_policy(self, bsr: bool, ratio_band: int, algo_flags: int) -> None:
         self.check(lib.setops_gpu_set_policy(self.handle, int(bsr), ratio_band, algo_flags))
 
@@ -426,20 +438,26 @@ class Server:
         self.ctx.check(lib.setops_srv_stats(self._h, *[C.byref(x) for x in v]))
         return dict(zip(("batches", "queries", "max_batch", "launches"), (x.value for x in v)))
 
-    def run_load(self, ids, ks, rate_qps: float, seed: int = 1):
-        """Open-loop Poisson load; returns (latency_ns[nq], counts[nq], elapsed_s)."""
+    def run_load(self, ids, ks, rate_qps: float, seed: int = 1, answer_stride: int = 0):
+        """Open-loop Poisson load; returns (latency_ns[nq], counts[nq],
+        elapsed_s), and with answer_stride > 0 also the answers themselves
+        (a list of arrays; each answer at most answer_stride long)."""
         ids = np.ascontiguousarray(ids, dtype=np.uint32)
         ks = np.ascontiguousarray(ks, dtype=np.uint32)
         nq = ks.size
         lat = np.zeros(nq, np.uint64)
         cnt = np.zeros(nq, np.uint64)
+        ans = np.zeros((nq, answer_stride), np.uint32) if answer_stride > 0 else None
         el = C.c_double()
         rc = lib.setops_srv_run_load(self._h, ids.ctypes.data, ks.ctypes.data, ids.shape[1], nq,
                                      rate_qps, seed, lat.ctypes.data, cnt.ctypes.data,
-                                     C.byref(el))
+                                     ans.ctypes.data if ans is not None else None,
+                                     answer_stride, C.byref(el))
         if rc != 0:
             raise SetopsError(rc, _lib.status_string(rc))
-        return lat, cnt, float(el.value)
+        if ans is None:
+            return lat, cnt, float(el.value)
+        return lat, cnt, float(el.value), [ans[q, :int(cnt[q])] for q in range(nq)]
 
     def stop(self) -> None:
         if self._h is not None:

@@ -67,6 +67,8 @@ SIGNATURES = [
     ("setops_gpu_last_error", C.c_char_p, [vp]),
     ("setops_gpu_num_variants", C.c_int, [uint, C.c_int]),
     ("setops_gpu_launch_count", u64, [vp]),
+    ("setops_gpu_set_wait_limit_ns", C.c_int, [vp, u64]),
+    ("setops_gpu_check_wait_limit", C.c_int, [vp, u64p]),
     ("setops_gpu_set_policy", C.c_int, [vp, C.c_int, C.c_int, uint]),
     ("setops_gpu_get_policy", C.c_int, [vp, C.c_int, C.c_int, C.POINTER(uint)]),
     ("setops_gpu_intersect_count", C.c_int, [vp, vp, sz, vp, sz, u64p, uint]),
@@ -99,8 +101,14 @@ SIGNATURES = [
     ("setops_srv_stats", C.c_int, [vp, u64p, u64p, u64p, u64p]),
     ("setops_srv_stop", C.c_int, [vp]),
     # setops_bench.h (the generators and datafile functions are listed in datasets.py)
-    ("setops_srv_run_load", C.c_int, [vp, vp, vp, sz, sz, C.c_double, u64, vp, vp,
+    ("setops_srv_run_load", C.c_int, [vp, vp, vp, sz, sz, C.c_double, u64, vp, vp, vp, sz,
                                       C.POINTER(C.c_double)]),
+    ("setops_bench_pairs_one_by_one", C.c_int, [vp, vp, vp, vp, vp, vp, sz, vp, vp, vp,
+                                                C.POINTER(C.c_double)]),
+    ("setops_bench_bsr_pairs_one_by_one", C.c_int, [vp, vp, vp, vp, vp, vp, vp, sz, vp, vp, vp,
+                                                    vp, C.POINTER(C.c_double)]),
+    ("setops_bench_queries_one_by_one", C.c_int, [vp, vp, vp, vp, vp, vp, sz, sz, vp, sz, vp,
+                                                  vp, C.POINTER(C.c_double)]),
 ]
 SIGNATURES += GEN_SIGNATURES
 

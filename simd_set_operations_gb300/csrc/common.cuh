@@ -25,7 +25,20 @@ enum DeviceError : int {
 // Wait limits, in nanoseconds of the GPU's global timer.  A bulk copy of a
 // few KB or a predecessor tile publishing its count takes microseconds; a
 // wait that reaches the limit records an error and the kernel returns.
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+constexpr uint64_t kDefaultWaitLimitNs = 2000000000ull;  // 2 s
+
+// The limit in force.  Without relocatable device code every translation
+// unit has its own copy (per device); setops_gpu_set_wait_limit_ns writes
+// all of them through the setters registered below.
+static __device__ uint64_t g_wait_limit_ns = kDefaultWaitLimitNs;
+
+__device__ __forceinline__ uint64_t wait_limit_ns() { return g_wait_limit_ns; }
+
+// Host side: each translation unit that includes this header registers a
+// setter of its own copy at static initialisation (the registry is in
+// runtime.cu).  A setter writes the copy on the current device.
+using WaitLimitSetter = cudaError_t (*)(uint64_t ns);
+void register_wait_limit_setter(WaitLimitSetter fn);
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -113,7 +126,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
   const uint64_t t0 = global_ns();
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (global_ns() - t0 > kWaitLimitNs) break;
+    if (global_ns() - t0 > wait_limit_ns()) break;
   }
   record_error(err, DEV_ERR_TIMEOUT_MBAR);
   return false;
@@ -131,7 +144,7 @@ __device__ __forceinline__ bool mbar_wait_abortable(uint64_t *bar,
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort) return false;
-    if (global_ns() - t0 > kWaitLimitNs) {
+    if (global_ns() - t0 > wait_limit_ns()) {
       record_error(err, DEV_ERR_TIMEOUT_MBAR);
       *abort = 1u;
       return false;
@@ -237,7 +250,7 @@ __device__ __forceinline__ uint64_t lookback_exclusive(uint64_t *status,
     if (e != (epoch & 0xffffu) || flag == 0) {
       if (t0 == 0) {
         t0 = global_ns();
-      } else if (global_ns() - t0 > kWaitLimitNs) {
+      } else if (global_ns() - t0 > wait_limit_ns()) {
         record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
         return UINT64_MAX;
       }
@@ -288,7 +301,7 @@ __device__ __forceinline__ uint64_t lookback_exclusive_warp(
     if (nrd & need) {
       if (t0 == 0) {
         t0 = global_ns();
-      } else if (global_ns() - t0 > kWaitLimitNs) {
+      } else if (global_ns() - t0 > wait_limit_ns()) {
         if (lane == 0) record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
         return UINT64_MAX;
       }
@@ -483,5 +496,11 @@ __device__ __forceinline__ uint64_t warp_start_below(const uint32_t *__restrict_
   warp_bracket_guess(B, n, keyp, est, &lo, &hi);
   return lo;
 }
+
+static cudaError_t set_wait_limit_this_unit(uint64_t ns) {
+  return cudaMemcpyToSymbol(g_wait_limit_ns, &ns, sizeof ns);
+}
+[[maybe_unused]] static const bool g_wait_limit_setter_registered =
+    (register_wait_limit_setter(&set_wait_limit_this_unit), true);
 
 }  // namespace setops

@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
       const uint64_t t0 = global_ns();
       while (ld_acquire_u64(reinterpret_cast<const uint64_t *>(&p.sync->acc)) == 0) {
         __nanosleep(100);
-        if (global_ns() - t0 > kWaitLimitNs) {
+        if (global_ns() - t0 > wait_limit_ns()) {
           record_error(p.err, DEV_ERR_TIMEOUT_LOOKBACK);
           ok = 0;
           break;

@@ -345,4 +345,21 @@ cudaError_t launch_bsr_decode(const uint32_t *bases, const uint32_t *states,
   return cudaGetLastError();
 }
 
+// One warp runs the look-back of tile 1 with tag `epoch`, whose predecessor
+// (tile 0) never publishes: status[0] holds no word of this tag.  The wait
+// therefore ends only by its time limit, which records
+// DEV_ERR_TIMEOUT_LOOKBACK; *waited gets the time the warp waited.
+__global__ void __launch_bounds__(32) wait_check_kernel(uint64_t *status, uint32_t epoch,
+                                                        int *err, uint64_t *waited) {
+  const uint64_t t0 = global_ns();
+  const uint64_t r = lookback_exclusive_warp(status, 1u, 1u, epoch, err);
+  if (threadIdx.x == 0) *waited = (r == UINT64_MAX) ? global_ns() - t0 : 0;
+}
+
+cudaError_t launch_wait_check(uint64_t *status, uint32_t epoch, int *err, uint64_t *waited,
+                              cudaStream_t st) {
+  wait_check_kernel<<<1, 32, 0, st>>>(status, epoch, err, waited);
+  return cudaGetLastError();
+}
+
 }  // namespace setops

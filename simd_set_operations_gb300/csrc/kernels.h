@@ -49,6 +49,10 @@ cudaError_t launch_bsr_decode(const uint32_t *bases, const uint32_t *states,
                               uint64_t *out_len, uint64_t *status,
                               LaunchSync *sync, int *err, uint32_t epoch,
                               int grid, cudaStream_t st);
+// A look-back wait that nothing ever satisfies (status[0..1] hold no word
+// of tag `epoch`), ended by the wait limit; *waited gets its duration.
+cudaError_t launch_wait_check(uint64_t *status, uint32_t epoch, int *err, uint64_t *waited,
+                              cudaStream_t st);
 constexpr int kBsrEncodeTile = 256 * 8;  // elements per encode tile
 constexpr int kBsrDecodeTile = 256 * 4;  // words per decode tile
 const void *bsr_encode_fn();

@@ -299,7 +299,7 @@ __device__ __forceinline__ uint64_t predecessor_sum(uint64_t *status,
     if (uint32_t(w >> 48) != ep) {
       const uint64_t t0 = global_ns();
       do {
-        if (global_ns() - t0 > kWaitLimitNs) {
+        if (global_ns() - t0 > wait_limit_ns()) {
           record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
           bad = true;
           break;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(
           v0 = w & kValueMask;
           break;
         }
-        if (global_ns() - t0 > kWaitLimitNs) {
+        if (global_ns() - t0 > wait_limit_ns()) {
           record_error(p.err, DEV_ERR_TIMEOUT_LOOKBACK);
           v0 = UINT64_MAX;
           break;

@@ -31,6 +31,17 @@ const char *kStatusText[] = {
 
 }  // namespace
 
+// Setters of the per-unit copies of the device wait limit (common.cuh).  A
+// function-local registry: units register during static initialisation.
+static std::vector<WaitLimitSetter> &wait_limit_setters() {
+  static std::vector<WaitLimitSetter> v;
+  return v;
+}
+
+void setops::register_wait_limit_setter(WaitLimitSetter fn) {
+  wait_limit_setters().push_back(fn);
+}
+
 int ctx_fail(setops_ctx *ctx, int status, const std::string &what) {
   if (ctx) ctx->err = what;
   return status;
@@ -473,6 +484,33 @@ int setops_gpu_num_variants(unsigned algo, int bsr) {
 
 uint64_t setops_gpu_launch_count(const setops_ctx *ctx) {
   return ctx ? ctx->launches : 0;
+}
+
+int setops_gpu_set_wait_limit_ns(setops_ctx *ctx, uint64_t ns) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if (ns == 0) ns = kDefaultWaitLimitNs;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->st));
+  for (WaitLimitSetter fn : wait_limit_setters()) CK(fn(ns));
+  CK(cudaDeviceSynchronize());
+  return SETOPS_OK;
+}
+
+int setops_gpu_check_wait_limit(setops_ctx *ctx, uint64_t *waited_ns) {
+  if (!ctx || !waited_ns) return SETOPS_ERR_INVALID;
+  *waited_ns = 0;
+  CK(cudaSetDevice(ctx->device));
+  RK(ctx_status_words(ctx, 2));
+  uint32_t epoch = 0;
+  RK(ctx_next_epoch(ctx, &epoch));  // a fresh tag: no status word carries it
+  uint64_t *status = static_cast<uint64_t *>(ctx->status.p);
+  CK(launch_wait_check(status, epoch, ctx->derr, ctx->dlen, ctx->st));
+  ++ctx->launches;
+  CK(cudaMemcpyAsync(&ctx->hres[1], ctx->dlen, sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                     ctx->st));
+  const int rc = ctx_check_device(ctx);  // synchronises; clears the error state
+  *waited_ns = ctx->hres[1];
+  return rc;
 }
 
 int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,

@@ -557,7 +557,8 @@ int setops_srv_stop(setops_srv *srv) {
 
 int setops_srv_run_load(setops_srv *srv, const uint32_t *ids, const uint32_t *ks,
                         size_t kstride, size_t nq, double rate_qps, uint64_t seed,
-                        uint64_t *latency_ns, uint64_t *counts, double *elapsed_s) {
+                        uint64_t *latency_ns, uint64_t *counts, uint32_t *answers,
+                        size_t answer_stride, double *elapsed_s) {
   if (!srv || !ids || !ks || !latency_ns || nq == 0 || rate_qps <= 0 || kstride < 2)
     return SETOPS_ERR_INVALID;
   std::mt19937_64 rng(seed);
@@ -585,6 +586,10 @@ int setops_srv_run_load(setops_srv *srv, const uint32_t *ids, const uint32_t *ks
       // open loop: latency counts from the query's scheduled arrival
       latency_ns[tag] = lat + (sent[tag] - (t0 + due[tag]));
       if (counts) counts[tag] = len;
+      if (answers) {
+        if (len > answer_stride) return SETOPS_ERR_CAPACITY;
+        std::memcpy(answers + tag * answer_stride, buf.data(), len * sizeof(uint32_t));
+      }
       ++got;
     }
   };

@@ -158,7 +158,7 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *arrived, uint32_t target,
     const uint64_t t0 = global_ns();
     while (ld_acquire_u32(arrived) < target) {
       __nanosleep(200);  // one load per CTA every few hundred ns
-      if (global_ns() - t0 > kWaitLimitNs) {
+      if (global_ns() - t0 > wait_limit_ns()) {
         record_error(err, DEV_ERR_TIMEOUT_LOOKBACK);
         ok = 0;
         break;

@@ -355,3 +355,21 @@ def test_batch_plan_replays(ctx, orc, generated):
     ctx.check(_lib.lib.setops_gpu_batch_plan_launch(plan))
     assert _lib.lib.setops_gpu_synchronize(ctx.handle) == _lib.ERR_CAPACITY
     ctx.check(_lib.lib.setops_gpu_batch_plan_destroy(plan))
+
+
+def test_batch_full_size_range_autotuned(ctx, orc):
+    """The batched configuration's full size range: 20,000 pairs with set
+    sizes log-uniform in [2^4, 2^16], density U[0.01, 0.5], selectivity
+    U[0, 0.5]; the policy autotuned on the batch, then every pair of one
+    launch equal to naive_merge of that pair, and the counts too."""
+    batch = ds.gen_batch(20240621, 20000, 16, 1 << 16)
+    assert int(max(batch.a_len.max(), batch.b_len.max())) > 1 << 15
+    want = expected(orc, batch)
+    v0, r0 = C.c_int(), C.c_uint32()
+    ctx.check(_lib.lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v0), C.byref(r0)))
+    try:
+        so.batch_autotune(batch.pool, batch.a_off, batch.a_len, batch.b_off, batch.b_len,
+                          reps=1, ctx=ctx)
+        check_batch(ctx, orc, batch, want)
+    finally:
+        ctx.check(_lib.lib.setops_gpu_batch_set_policy(ctx.handle, v0.value, r0.value))

@@ -234,3 +234,27 @@ def test_default_policy_bands(ctx, orc):
         want = orc.naive_merge(a, b)
         out, n = so.intersect(a, b, ctx=ctx)
         assert np.array_equal(out[:n], want), ratio
+
+
+def test_config0_plain_pair(ctx, orc):
+    """The plain 2-set configuration at its exact shape: |A| = |B| = 2^20,
+    element space 2^20 / 0.1, selectivity 0.1 (the reference's gen_twoset,
+    benchmark/src/generators.rs:30-68).  Count and materialised output of the
+    default policy and of every merge and bitmap variant, through host and
+    device pointers, equal naive_merge (setops/src/intersect/merge.rs:7-33)."""
+    import torch
+    a, b = ds.gen_twoset(20240620, 0.1, 0.1, 1 << 20, 1 << 20)
+    want = orc.naive_merge(a, b)
+    assert want.size == int(0.1 * (1 << 20))
+    algos = [so.ALGO_AUTO]
+    algos += [so.ALGO_MERGE | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_MERGE))]
+    algos += [so.ALGO_BITMAP | so.VARIANT(v) for v in range(so.num_variants(so.ALGO_BITMAP))]
+    check_pair(ctx, orc, a, b, algos)
+    ta = torch.from_numpy(a.view(np.int32)).cuda()
+    tb = torch.from_numpy(b.view(np.int32)).cuda()
+    for algo in algos:
+        out, n = so.intersect(ta, tb, algo=algo, ctx=ctx)
+        got = out[:n].cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, want), hex(algo)
+        out, n = so.intersect(tb, ta, algo=algo, ctx=ctx)  # operands swapped
+        assert np.array_equal(out[:n].cpu().numpy().view(np.uint32), want), hex(algo)

@@ -61,10 +61,16 @@ def test_serve_poisson_load(ctx, orc, index, queries):
     want = oracle_answers(orc, index, ids, ks)
     reps = 5
     ids_r, ks_r = np.tile(ids, (reps, 1)), np.tile(ks, reps)
+    stride = max(max(w.size for w in want), 1)
     with so.Server(index.pool, index.offs, index.lens, budget=16 << 20, ctx=ctx) as srv:
-        lat, cnt, el = srv.run_load(ids_r, ks_r, rate_qps=20000, seed=3)
+        lat, cnt, el, answers = srv.run_load(ids_r, ks_r, rate_qps=200000, seed=3,
+                                             answer_stride=stride)
+        st = srv.stats()
     assert el > 0 and np.all(lat > 0)
+    assert st["max_batch"] > 1, st  # queries arriving under load were batched together
     assert [int(c) for c in cnt] == [w.size for w in want] * reps
+    for q, got in enumerate(answers):  # every answer under load, element by element
+        assert np.array_equal(got, want[q % ks.size]), q
 
 
 def test_serve_rejects_bad_queries(ctx, index):

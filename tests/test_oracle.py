@@ -147,3 +147,41 @@ def test_run_pairs_threads(orc):
     groups = [[rand_set(rng, 300, 2000) for _ in range(3)] for _ in range(10)]
     wantk = np.array([orc.svs_generic(g).size for g in groups], np.uint64)
     assert np.array_equal(orc.run_svs_groups(groups, 3), wantk)
+
+
+def test_svs_with_each_baseline_equals_svs_generic(orc):
+    """svs_generic run with each timed CPU baseline as its 2-set function
+    gives svs_generic's (naive_merge) result."""
+    rng = np.random.default_rng(33)
+    core = np.sort(rng.choice(1 << 20, 300, replace=False)).astype(np.uint32)
+    groups = []
+    for k in (2, 3, 5):
+        g = []
+        for i in range(k):
+            extra = rng.choice(1 << 20, 4000 // (i + 1), replace=False).astype(np.uint32)
+            g.append(np.unique(np.concatenate([core, extra])))
+        groups.append(sorted(g, key=len))
+    want = [orc.svs_generic(g) for g in groups]
+    for algo in (orc.SHUFFLING_W8, orc.SIMD_GALLOPING_W16, orc.BMISS_W4, orc.BRANCHLESS_MERGE):
+        outs = [np.empty(min(s.size for s in g), np.uint32) for g in groups]
+        counts = orc.run_svs_groups(groups, 2, outs=outs, algo=algo)
+        for w, o, c in zip(want, outs, counts):
+            assert np.array_equal(o[:int(c)], w), orc.ALGO_NAMES[algo]
+
+
+def test_bsr_pair_runner_equals_single_calls(orc):
+    rng = np.random.default_rng(44)
+    pairs, want = [], []
+    for n in (0, 1, 50, 3000):
+        a = np.unique(rng.integers(0, 1 << 14, n)).astype(np.uint32)
+        b = np.unique(rng.integers(0, 1 << 14, 2 * n + 1)).astype(np.uint32)
+        ba, sa = orc.bsr_from_sorted(a)
+        bb, sb = orc.bsr_from_sorted(b)
+        pairs.append((ba, sa, bb, sb))
+        want.append(orc.branchless_merge_bsr(ba, sa, bb, sb))
+    for algo in (0, 1):
+        outs = [(np.empty(max(p[0].size, 1), np.uint32), np.empty(max(p[0].size, 1), np.uint32))
+                for p in pairs]
+        words = orc.run_bsr_pairs(pairs, 3, outs=outs, algo=algo)
+        for (wb, ws), (ob, os_), w in zip(want, outs, words):
+            assert np.array_equal(ob[:int(w)], wb) and np.array_equal(os_[:int(w)], ws)
