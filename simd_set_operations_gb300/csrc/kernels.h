@@ -31,6 +31,9 @@ int num_variants(Algo algo, bool bsr);
 // SETOPS_ALGO_BITMAP variant with coarse bitmaps for sparse tiles (the
 // default for size ratios 2-31 and for SvS steps below the search ratio)
 constexpr int kCoarseBitmap = 7;
+// SETOPS_ALGO_BITMAP variant whose materialise kernel stages both inputs in
+// shared memory by asynchronous copies (the default for size ratios below 2)
+constexpr int kStagedWindow = 8;
 // The fused k-set kernel (kset.cuh): count or materialise.
 const KernelInfo &kset_kernel(bool mat);
 constexpr int kKsetThreads = 128;

@@ -220,7 +220,7 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
   // 2^22 its larger shared-memory footprint costs a few per cent on dense
   // pairs)
   if (!bsr && band == 0 && !(ctx->policy_user[0] & 1u) && c.algo == ALGO_BITMAP &&
-      c.variant == 0 && mn <= (uint64_t(1) << 22))
+      c.variant == kStagedWindow && mn <= (uint64_t(1) << 22))
     c.variant = kCoarseBitmap;
   return c;
 }
@@ -237,8 +237,9 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // arrays: ratio < 2: tiled bitmap (ctx_choose takes variant 7 for pairs
-    // of at most 2^22 under this default); 2..31: tiled bitmap with coarse
+    // arrays: ratio < 2: tiled bitmap, inputs staged in shared memory
+    // (variant 8; ctx_choose takes variant 7 for pairs of at most 2^22
+    // under this default); 2..31: tiled bitmap with coarse
     // bitmaps for sparse tiles (variant 7); 32..511: sampled
     // thread-per-element search; 512..8191: 8 lanes per element (4 elements
     // a warp); >= 8192: a warp per element.  BSR: merge-path below 32.
@@ -248,7 +249,7 @@ void ctx_default_policy(setops_ctx *ctx) {
                  : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
                  : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3))
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
-    unsigned u = (b < 1)   ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(0))
+    unsigned u = (b < 1)   ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kStagedWindow))
                  : (b < 5) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kCoarseBitmap))
                            : v,
              s = v;
@@ -538,6 +539,37 @@ int setops_gpu_get_policy(const setops_ctx *ctx, int bsr, int ratio_band,
 
 // ---- 2-set arrays ----
 
+// The device address of host memory the GPU can read in place (pinned by
+// cudaHostAlloc or registered, so mapped into the device's address space),
+// else nullptr (pageable memory).
+static void *device_view(const void *h) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return (at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
+}
+
+// Host inputs the kernels read in place instead of copying them first: on
+// this machine the host link (NVLink-C2C, about 210 GB/s) is the bound of a
+// host-pointer call either way, and reading in place moves only what the
+// kernel touches.  Taken when both inputs are device-readable host memory
+// and the chosen kernel reads its inputs with plain loads (the merge-path
+// kernel and the staged window variant copy them with asynchronous copies:
+// those pairs are copied first), and -- for the search kernel -- when its
+// probes touch at most a quarter of the larger input's 32-byte sectors (an
+// estimate: per small element, the levels of a search over a gap of
+// max/min elements whose probes are more than one sector apart).
+static bool read_in_place(const Choice &c, uint64_t mn, uint64_t mx) {
+  if (c.algo == ALGO_MERGE) return false;
+  if (c.algo == ALGO_BITMAP) return true;
+  int lvl = 0;
+  for (uint64_t g = mx / (mn ? mn : 1); g > 1; g >>= 1) ++lvl;
+  const uint64_t sectors = mn * uint64_t(lvl > 3 ? lvl - 2 : 1);
+  return sectors * 32 <= mx;  // a quarter of the larger input's 4 * mx bytes
+}
+
 static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
                           const uint32_t *b, size_t nb, uint32_t *out,
                           size_t out_cap, uint64_t *len_host,
@@ -555,15 +587,28 @@ static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
   CK(cudaSetDevice(ctx->device));
   const uint32_t *da = a, *db = b;
   uint32_t *dout = out;
+  Choice choice = ctx_choose(ctx, na, nb, false, flags);
+  bool out_in_place = false;
   if (host) {
     if (len_dev_user) return ctx_fail(ctx, SETOPS_ERR_INVALID, "async call with host pointers");
-    if (mn > 0) {
+    void *va = mn ? device_view(a) : nullptr, *vb = mn ? device_view(b) : nullptr;
+    if (va && vb && read_in_place(choice, mn, std::max<uint64_t>(na, nb))) {
+      da = static_cast<const uint32_t *>(va);
+      db = static_cast<const uint32_t *>(vb);
+      if (choice.algo == ALGO_BITMAP && choice.variant == kStagedWindow) choice.variant = 0;
+    } else if (mn > 0) {
       RK(ctx_stage_in(ctx, 0, a, na, &da));
       RK(ctx_stage_in(ctx, 1, b, nb, &db));
     }
     if (mat) {
-      RK(buf_reserve(ctx, ctx->out0, std::max<uint64_t>(mn, 1) * 4));
-      dout = static_cast<uint32_t *>(ctx->out0.p);
+      void *vo = mn ? device_view(out) : nullptr;
+      if (vo) {  // the kernel writes the result straight into host memory
+        dout = static_cast<uint32_t *>(vo);
+        out_in_place = true;
+      } else {
+        RK(buf_reserve(ctx, ctx->out0, std::max<uint64_t>(mn, 1) * 4));
+        dout = static_cast<uint32_t *>(ctx->out0.p);
+      }
     }
   }
   uint64_t *len_dev = len_dev_user ? len_dev_user : &ctx->dlen[0];
@@ -583,12 +628,12 @@ static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
   j.out = mat ? dout : nullptr;
   j.out_cap = mat ? out_cap : 0;
   j.len_dev = len_dev;
-  j.choice = ctx_choose(ctx, na, nb, false, flags);
+  j.choice = choice;
   RK(ctx_launch_pair(ctx, j));
   if (len_dev_user) return SETOPS_OK;
   uint64_t n = 0;
   RK(ctx_read_u64(ctx, len_dev, &n));
-  if (host && mat && n > 0) {
+  if (host && mat && n > 0 && !out_in_place) {
     CK(cudaMemcpyAsync(out, dout, n * 4, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
   }

@@ -213,13 +213,14 @@ def test_visitor_api(ctx, orc):
 
 def test_default_policy_bands(ctx, orc):
     """The default policy per floor(log2(max/min)) band: arrays take the
-    window kernel below ratio 2, its coarse-bitmap variant (7) for 2-31, then
+    window kernel with staged inputs (8) below ratio 2, its coarse-bitmap
+    variant (7) for 2-31, then
     the search kernel (sampled, 8-lane, warp per element); BSR pairs take the
     merge path below 32.  Each band's choice gives the oracle's result on a
     pair of that ratio."""
     def algo_var(flags):
         return flags & 0xFF00, (flags >> 16) & 0xFF  # (algorithm bits, variant)
-    want_arr = {0: (so.ALGO_BITMAP, 0), 1: (so.ALGO_BITMAP, 7), 4: (so.ALGO_BITMAP, 7),
+    want_arr = {0: (so.ALGO_BITMAP, 8), 1: (so.ALGO_BITMAP, 7), 4: (so.ALGO_BITMAP, 7),
                 5: (so.ALGO_GALLOP, 0), 8: (so.ALGO_GALLOP, 0), 9: (so.ALGO_GALLOP, 3),
                 12: (so.ALGO_GALLOP, 3), 13: (so.ALGO_GALLOP, 2), 20: (so.ALGO_GALLOP, 2)}
     for band, (algo, var) in want_arr.items():
@@ -258,3 +259,32 @@ def test_config0_plain_pair(ctx, orc):
         assert np.array_equal(got, want), hex(algo)
         out, n = so.intersect(tb, ta, algo=algo, ctx=ctx)  # operands swapped
         assert np.array_equal(out[:n].cpu().numpy().view(np.uint32), want), hex(algo)
+
+
+def _pinned(x: np.ndarray) -> np.ndarray:
+    import torch
+    t = torch.empty(max(x.size, 1), dtype=torch.int32).pin_memory()
+    v = t.numpy().view(np.uint32)[:x.size]
+    v[:] = x
+    return v  # (the view's base holds the pinned tensor)
+
+
+def test_pinned_host_inputs_read_in_place(ctx, orc):
+    """Host-pointer calls on pinned host memory: the kernels read the inputs
+    in place (and write the result straight into a pinned output) where the
+    chosen kernel allows it, else copy them first.  Every shape, count and
+    materialised, pinned or pageable output, equals naive_merge."""
+    rng = np.random.default_rng(31)
+    shapes = [(200_000, 200_000, 2_000), (70_000, 210_000, 700), (1_000, 1 << 18, 10),
+              (1 << 14, 1 << 22, 160), (1 << 18, 1 << 22, 2_600), (5, 3, 1)]
+    for na, nb, shared in shapes:
+        a, b = pair_with_overlap(rng, na, nb, shared)
+        want = orc.naive_merge(a, b)
+        pa, pb = _pinned(a), _pinned(b)
+        for algo in (so.ALGO_AUTO, so.ALGO_BITMAP, so.ALGO_GALLOP, so.ALGO_MERGE):
+            for pinned_out in (True, False):
+                cap = min(na, nb)
+                out = _pinned(np.zeros(cap, np.uint32)) if pinned_out else np.zeros(cap, np.uint32)
+                got, n = so.intersect(pa, pb, out, algo=algo, ctx=ctx)
+                assert np.array_equal(got[:n], want), (na, nb, hex(algo), pinned_out)
+            assert so.intersect_count(pa, pb, algo=algo, ctx=ctx) == want.size
