@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--bsr-pairs", type=int, default=10000,
                    help="pairs of the BSR subset of the batch leg")
     p.add_argument("--no-kset", action="store_true", help="skip the k-set leg")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the hand-written policy table (no tuning before the sweep)")
     p.add_argument("--no-config0", action="store_true",
                    help="skip the plain 2^20 x 2^20 pair leg")
     p.add_argument("--no-serve", action="store_true",
@@ -1097,6 +1099,14 @@ def summarize(roofline, e2e, cpu, config0, batch, kset, serve) -> dict:
     return out
 
 
+KERNEL_NAMES = {
+    "bitmap/0": "window_kernel (bitmap tiles, B in register windows)",
+    "bitmap/7": "window_kernel, coarse bitmaps for sparse tiles",
+    "bitmap/8": "awindow_kernel (bitmap tiles, A tiles and B windows staged in shared memory "
+                "by cp.async)",
+}
+
+
 def run_gb300(args):
     import ctypes as C
 
@@ -1117,6 +1127,19 @@ def run_gb300(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream)
     L = _lib.lib
+
+    # the array policy, tuned on this GPU before anything is timed (bands up
+    # to 2^16 : 1, test pairs of up to 2^25 elements, the sweep's density)
+    policy = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tab = so.autotune(band_lo=0, band_hi=16, max_elems=1 << 25, density=DENSITY, reps=3,
+                          ctx=ctx)
+        policy = {"tuned_cells": tab["tuned_cells"], "seconds": time.perf_counter() - t0,
+                  "device": tab["key"]["device"],
+                  "table": {cell: so.describe_flags(f) for cell, f in tab["cells"].items()},
+                  "note": "cell 'band,class': size ratio in [2^band, 2^(band+1)), smaller "
+                          "input < 2^12 / 2^16 / 2^22 / above (class 0-3)"}
 
     sel = [int(x) for x in args.pairs.split(",")]
     pairs = [p for i, p in enumerate(make_sweep(rank)) if i in sel]
@@ -1218,10 +1241,11 @@ def run_gb300(args):
     achieved = algo_bytes / (head_ms / 1e3) / 1e9
     peak, peak_kind = read_peak()
     traffic = read_traffic()
+    head_flags = ctx.get_policy_class(False, 0, 3)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "awindow_kernel (bitmap tiles, A tiles and B windows staged in "
-                          "shared memory by cp.async; 2^24 x 2^24 pair, materialise)",
+                "kernel": f"{KERNEL_NAMES.get(so.describe_flags(head_flags), so.describe_flags(head_flags))}"
+                          " (2^24 x 2^24 pair, materialise)",
                 "algorithmic_bytes_per_launch": algo_bytes,
                 "launch_ms_mean": head_ms, "peak_source": f"{peak_kind} (hbm_gbs)"}
     sweep = []
@@ -1271,23 +1295,19 @@ def run_gb300(args):
         e_el = max_over_ranks(e_el)
         h2d = sum(4 * (s.size + l.size) for s, l in pairs)
         d2h = 4 * tot_out + 8 * len(pairs)
-        # what crosses the host link: a pair read in place by a search moves
-        # only the sectors its probes touch (the library reads a search-band
-        # pair in place when that is at most a quarter of the larger input)
+        # what crosses the host link: a search-band pair is read in place and
+        # moves only the sectors its probes touch; a balanced pair is copied
         moved = 0
         for s, l in pairs:
-            tb = touched_bytes(s.size, l.size, int(SELECTIVITY * s.size))
-            moved += tb if (l.size >= 32 * s.size and tb - 4 * s.size <= l.size) \
-                else 4 * (s.size + l.size)
+            moved += touched_bytes(s.size, l.size, int(SELECTIVITY * s.size)) \
+                if l.size >= 32 * s.size else 4 * (s.size + l.size)
         e2e = {"value": job_value(world, len(pairs), e2e_steps, e_el), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "ms_per_step": 1e3 * e_el / e2e_steps,
                "h2d_bytes_moved_est": moved,
-               "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers: the "
-                      "kernels read pinned inputs in place over the host link (NVLink-C2C) "
-                      "and write the result into the pinned output, except where copying "
-                      "first is cheaper (a search touching more than a quarter of the "
-                      "larger set)"}
+               "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers: "
+                      "search-band pairs are read in place over the host link (NVLink-C2C), "
+                      "balanced pairs copied first; results written into the pinned output"}
 
     # CPU baseline (rank 0 at N=1 only), also the cross-check of the results
     cpu = None
@@ -1334,7 +1354,8 @@ def run_gb300(args):
         "data": "synthetic (seeded; reference generator shape)",
         "config": workload_config(sel),
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": int(launches), "clocks": clocks, "sweep": sweep, "config0": config0,
+        "gpu_launches": int(launches), "clocks": clocks, "policy": policy, "sweep": sweep,
+        "config0": config0,
         "batch": batch, "kset": kset, "serve": serve,
         "timing": {"bracket_ms_total": wall_ms, "headline_ms_total": sum(head_times),
                    "note": "value = pairs / CUDA-event time of the K-step bracket (no host "

@@ -113,6 +113,31 @@ int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
                           unsigned algo_flags);
 int setops_gpu_get_policy(const setops_ctx *ctx, int bsr, int ratio_band,
                           unsigned *algo_flags);
+/* The policy table is kept per size class of the pair's smaller input as
+ * well: [0, 2^12), [2^12, 2^16), [2^16, 2^22) and [2^22, ...) elements
+ * (size_class 0-3).  setops_gpu_set_policy sets a band's four classes at
+ * once and setops_gpu_get_policy reads its class 3; these set and read one
+ * cell. */
+#define SETOPS_SIZE_CLASSES 4
+int setops_gpu_set_policy_class(setops_ctx *ctx, int bsr, int ratio_band, int size_class,
+                                unsigned algo_flags);
+int setops_gpu_get_policy_class(const setops_ctx *ctx, int bsr, int ratio_band,
+                                int size_class, unsigned *algo_flags);
+/* The autotuner of the array table (the reference's counterpart is its
+ * compile-time choice of algorithm per instruction set,
+ * setops/src/intersect.rs:26-36).  For every ratio band in [band_lo,
+ * band_hi] and size class whose test pair fits max_elems elements (smaller
+ * set 2^10, 2^14, 2^19 or 2^23 elements, larger 1.4 * 2^band times that),
+ * generates a seeded pair at `density` with 1 % matches, times every
+ * algorithm and kernel variant on it (reps back-to-back materialising
+ * launches, CUDA events), requires every candidate to find the same number
+ * of matches (else SETOPS_ERR_CUDA), and writes the fastest into the table.
+ * *tuned (optional) gets the number of cells written.  Takes seconds; run it
+ * once per GPU and keep the table (setops_gpu_get_policy_class). */
+int setops_gpu_autotune(setops_ctx *ctx, int band_lo, int band_hi, size_t max_elems,
+                        double density, int reps, int *tuned);
+/* A text naming the GPU and driver (for keying a saved policy table). */
+int setops_gpu_device_key(setops_ctx *ctx, char *buf, size_t cap);
 
 /* ---- 2-set, u32 arrays --------------------------------------------------
  * Replace `Intersect2<[u32], V> = fn(&[u32], &[u32], &mut V)`

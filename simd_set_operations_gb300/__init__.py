@@ -44,6 +44,7 @@ __all__ = [
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
     "batch_intersect", "batch_count", "batch_intersect_bsr", "batch_count_bsr", "batch_autotune",
+    "autotune", "describe_flags", "SIZE_CLASSES",
     "Server",
 ]
 
@@ -116,6 +117,22 @@ class Context:
         v = C.c_uint()
         self.check(lib.setops_gpu_get_policy(self.handle, int(bsr), ratio_band, C.byref(v)))
         return v.value
+
+    def get_policy_class(self, bsr: bool, ratio_band: int, size_class: int) -> int:
+        v = C.c_uint()
+        self.check(lib.setops_gpu_get_policy_class(self.handle, int(bsr), ratio_band, size_class,
+                                                   C.byref(v)))
+        return v.value
+
+    def set_policy_class(self, bsr: bool, ratio_band: int, size_class: int,
+                         algo_flags: int) -> None:
+        self.check(lib.setops_gpu_set_policy_class(self.handle, int(bsr), ratio_band, size_class,
+                                                   algo_flags))
+
+    def device_key(self) -> str:
+        buf = C.create_string_buffer(256)
+        self.check(lib.setops_gpu_device_key(self.handle, buf, 256))
+        return buf.value.decode()
 
 
 _default: Context | None = None
@@ -376,6 +393,50 @@ def batch_autotune(pool, a_off, a_len, b_off, b_len, *, reps: int = 3,
     v, r = C.c_int(), C.c_uint32()
     ctx.check(lib.setops_gpu_batch_get_policy(ctx.handle, C.byref(v), C.byref(r)))
     return int(v.value), int(r.value)
+
+
+SIZE_CLASSES = 4  # SETOPS_SIZE_CLASSES: smaller input < 2^12, < 2^16, < 2^22, larger
+
+
+def autotune(*, band_lo: int = 0, band_hi: int = 16, max_elems: int = 1 << 25,
+             density: float = 0.05, reps: int = 3, cache: str | None = None,
+             ctx: Context | None = None) -> dict:
+    """Fills the context's array policy table (algorithm and kernel variant
+    per size-ratio band and size class) by timing every candidate on
+    generated pairs (setops_gpu_autotune), and returns the table.  With
+    `cache` (a JSON file), a table saved there for the same GPU, driver and
+    tuning arguments is applied instead of tuning, and a new one is saved."""
+    import json
+    import os
+    ctx = ctx or default_context()
+    key = {"device": ctx.device_key(), "band_lo": band_lo, "band_hi": band_hi,
+           "max_elems": int(max_elems), "density": float(density)}
+    if cache and os.path.exists(cache):
+        try:
+            saved = json.load(open(cache))
+        except (OSError, ValueError):
+            saved = None
+        if saved and saved.get("key") == key:
+            for cell, flags in saved["cells"].items():
+                band, cls = (int(x) for x in cell.split(","))
+                ctx.set_policy_class(False, band, cls, int(flags))
+            return dict(saved, from_cache=True)
+    n = C.c_int()
+    ctx.check(lib.setops_gpu_autotune(ctx.handle, band_lo, band_hi, int(max_elems),
+                                      float(density), reps, C.byref(n)))
+    cells = {f"{b},{c}": ctx.get_policy_class(False, b, c)
+             for b in range(band_lo, band_hi + 1) for c in range(SIZE_CLASSES)}
+    table = {"key": key, "tuned_cells": int(n.value), "cells": cells, "from_cache": False}
+    if cache:
+        with open(cache, "w") as f:
+            json.dump(table, f, indent=1)
+    return table
+
+
+def describe_flags(flags: int) -> str:
+    """'bitmap/8', 'gallop/3', ... for a policy entry."""
+    names = {ALGO_MERGE: "merge", ALGO_GALLOP: "gallop", ALGO_BITMAP: "bitmap"}
+    return f"{names.get(flags & 0xFF00, '?')}/{(flags >> 16) & 0xFF}"
 
 
 # ---------------------------------------------------------------------------

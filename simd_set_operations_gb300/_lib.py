@@ -71,6 +71,11 @@ SIGNATURES = [
     ("setops_gpu_check_wait_limit", C.c_int, [vp, u64p]),
     ("setops_gpu_set_policy", C.c_int, [vp, C.c_int, C.c_int, uint]),
     ("setops_gpu_get_policy", C.c_int, [vp, C.c_int, C.c_int, C.POINTER(uint)]),
+    ("setops_gpu_set_policy_class", C.c_int, [vp, C.c_int, C.c_int, C.c_int, uint]),
+    ("setops_gpu_get_policy_class", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.POINTER(uint)]),
+    ("setops_gpu_autotune", C.c_int, [vp, C.c_int, C.c_int, sz, C.c_double, C.c_int,
+                                      C.POINTER(C.c_int)]),
+    ("setops_gpu_device_key", C.c_int, [vp, C.c_char_p, sz]),
     ("setops_gpu_intersect_count", C.c_int, [vp, vp, sz, vp, sz, u64p, uint]),
     ("setops_gpu_intersect", C.c_int, [vp, vp, sz, vp, sz, vp, sz, szp, uint]),
     ("setops_gpu_intersect_async", C.c_int, [vp, vp, sz, vp, sz, vp, sz, vp, uint]),

@@ -209,19 +209,12 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
   }
   int band = 0;
   for (uint64_t r = mx / mn; r > 1 && band < kRatioBands - 1; r >>= 1) ++band;
-  const unsigned pol = ctx->policy[bsr ? 1 : 0][band];
+  const unsigned pol = ctx->policy[bsr ? 1 : 0][band][size_class(mn)];
   const unsigned pa = pol & SETOPS_ALGO_MASK;
   c.algo = (pa == SETOPS_ALGO_GALLOP)               ? ALGO_GALLOP
            : (pa == SETOPS_ALGO_BITMAP && !bsr)     ? ALGO_BITMAP
                                                     : ALGO_MERGE;
   c.variant = int((pol & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
-  // default balanced band, arrays of at most 2^22: the coarse-bitmap variant
-  // (the same time on dense pairs there, about half on sparse ones; above
-  // 2^22 its larger shared-memory footprint costs a few per cent on dense
-  // pairs)
-  if (!bsr && band == 0 && !(ctx->policy_user[0] & 1u) && c.algo == ALGO_BITMAP &&
-      c.variant == kStagedWindow && mn <= (uint64_t(1) << 22))
-    c.variant = kCoarseBitmap;
   return c;
 }
 
@@ -229,7 +222,7 @@ Choice ctx_choose(const setops_ctx *ctx, uint64_t na, uint64_t nb, bool bsr,
 // kernel (used for device-side choices).
 uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
   for (int band = 0; band < kRatioBands; ++band)
-    if ((ctx->policy[bsr ? 1 : 0][band] & SETOPS_ALGO_MASK) ==
+    if ((ctx->policy[bsr ? 1 : 0][band][kSizeClasses - 1] & SETOPS_ALGO_MASK) ==
         SETOPS_ALGO_GALLOP)
       return 1u << band;
   return 0xffffffffu;
@@ -237,9 +230,7 @@ uint32_t ctx_search_threshold(const setops_ctx *ctx, bool bsr) {
 
 void ctx_default_policy(setops_ctx *ctx) {
   for (int b = 0; b < kRatioBands; ++b) {
-    // arrays: ratio < 2: tiled bitmap, inputs staged in shared memory
-    // (variant 8; ctx_choose takes variant 7 for pairs of at most 2^22
-    // under this default); 2..31: tiled bitmap with coarse
+    // arrays: ratio < 32: tiled bitmap with coarse
     // bitmaps for sparse tiles (variant 7); 32..511: sampled
     // thread-per-element search; 512..8191: 8 lanes per element (4 elements
     // a warp); >= 8192: a warp per element.  BSR: merge-path below 32.
@@ -249,13 +240,17 @@ void ctx_default_policy(setops_ctx *ctx) {
                  : (b < 9)  ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
                  : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(3))
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
-    unsigned u = (b < 1)   ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kStagedWindow))
-                 : (b < 5) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kCoarseBitmap))
-                           : v,
-             s = v;
-    ctx->policy[0][b] = u;
-    ctx->policy[1][b] = s;
+    unsigned u = (b < 5) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kCoarseBitmap)) : v;
+    for (int c = 0; c < kSizeClasses; ++c) {
+      ctx->policy[0][b][c] = u;
+      ctx->policy[1][b][c] = v;
+    }
   }
+  // the balanced band's largest pairs: the window kernel with both inputs
+  // staged in shared memory (the coarse-bitmap variant's second table costs
+  // a few per cent on dense pairs there; below 2^22 the two are equal on
+  // dense pairs and the coarse one about twice as fast on sparse ones)
+  ctx->policy[0][0][kSizeClasses - 1] = SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kStagedWindow);
 }
 
 // ---------------------------------------------------------------------------
@@ -523,9 +518,30 @@ int setops_gpu_set_policy(setops_ctx *ctx, int bsr, int ratio_band,
   const int v = int((algo_flags & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
   const Algo al = a == SETOPS_ALGO_MERGE ? ALGO_MERGE : a == SETOPS_ALGO_GALLOP ? ALGO_GALLOP : ALGO_BITMAP;
   if (v >= num_variants(al, bsr != 0)) return SETOPS_ERR_INVALID;
-  ctx->policy[bsr ? 1 : 0][ratio_band] =
-      algo_flags & (SETOPS_ALGO_MASK | SETOPS_VARIANT_MASK);
-  ctx->policy_user[bsr ? 1 : 0] |= 1u << ratio_band;
+  for (int c = 0; c < kSizeClasses; ++c)
+    ctx->policy[bsr ? 1 : 0][ratio_band][c] = algo_flags & (SETOPS_ALGO_MASK | SETOPS_VARIANT_MASK);
+  return SETOPS_OK;
+}
+
+int setops_gpu_set_policy_class(setops_ctx *ctx, int bsr, int ratio_band, int size_class,
+                                unsigned algo_flags) {
+  if (!ctx || size_class < 0 || size_class >= kSizeClasses) return SETOPS_ERR_INVALID;
+  unsigned keep[kSizeClasses];
+  std::memcpy(keep, ctx->policy[bsr ? 1 : 0][ratio_band < 0 ? 0 : ratio_band % kRatioBands],
+              sizeof keep);
+  RK(setops_gpu_set_policy(ctx, bsr, ratio_band, algo_flags));  // validates
+  const unsigned f = ctx->policy[bsr ? 1 : 0][ratio_band][size_class];
+  std::memcpy(ctx->policy[bsr ? 1 : 0][ratio_band], keep, sizeof keep);
+  ctx->policy[bsr ? 1 : 0][ratio_band][size_class] = f;
+  return SETOPS_OK;
+}
+
+int setops_gpu_get_policy_class(const setops_ctx *ctx, int bsr, int ratio_band, int size_class,
+                                unsigned *algo_flags) {
+  if (!ctx || !algo_flags || ratio_band < 0 || ratio_band >= kRatioBands || size_class < 0 ||
+      size_class >= kSizeClasses)
+    return SETOPS_ERR_INVALID;
+  *algo_flags = ctx->policy[bsr ? 1 : 0][ratio_band][size_class];
   return SETOPS_OK;
 }
 
@@ -533,7 +549,7 @@ int setops_gpu_get_policy(const setops_ctx *ctx, int bsr, int ratio_band,
                           unsigned *algo_flags) {
   if (!ctx || !algo_flags || ratio_band < 0 || ratio_band >= kRatioBands)
     return SETOPS_ERR_INVALID;
-  *algo_flags = ctx->policy[bsr ? 1 : 0][ratio_band];
+  *algo_flags = ctx->policy[bsr ? 1 : 0][ratio_band][kSizeClasses - 1];
   return SETOPS_OK;
 }
 
@@ -551,24 +567,17 @@ static void *device_view(const void *h) {
   return (at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
 }
 
-// Host inputs the kernels read in place instead of copying them first: on
-// this machine the host link (NVLink-C2C, about 210 GB/s) is the bound of a
-// host-pointer call either way, and reading in place moves only what the
-// kernel touches.  Taken when both inputs are device-readable host memory
-// and the chosen kernel reads its inputs with plain loads (the merge-path
-// kernel and the staged window variant copy them with asynchronous copies:
-// those pairs are copied first), and -- for the search kernel -- when its
-// probes touch at most a quarter of the larger input's 32-byte sectors (an
-// estimate: per small element, the levels of a search over a gap of
-// max/min elements whose probes are more than one sector apart).
-static bool read_in_place(const Choice &c, uint64_t mn, uint64_t mx) {
-  if (c.algo == ALGO_MERGE) return false;
-  if (c.algo == ALGO_BITMAP) return true;
-  int lvl = 0;
-  for (uint64_t g = mx / (mn ? mn : 1); g > 1; g >>= 1) ++lvl;
-  const uint64_t sectors = mn * uint64_t(lvl > 3 ? lvl - 2 : 1);
-  return sectors * 32 <= mx;  // a quarter of the larger input's 4 * mx bytes
-}
+// Host inputs a search reads in place instead of copying them first.  On
+// this machine the host link (NVLink-C2C) moves about 210 GB/s, by copy or by
+// a kernel reading pinned memory, so a host-pointer call is bound by the
+// bytes it moves: a search reads only the sectors its probes touch (2^10 to
+// 2^18 elements against 2^24: 0.04-0.28 ms in place against 0.31-0.37 ms
+// with the 64 MB larger set copied first), while a balanced pair reads both
+// inputs whole and the window kernel streams host memory slower than a copy
+// (0.89 against 0.66 ms for 2^24 x 2^24).  So: search-band pairs whose
+// inputs are both device-readable host memory are read in place; everything
+// else is copied.
+static bool read_in_place(const Choice &c) { return c.algo == ALGO_GALLOP; }
 
 static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
                           const uint32_t *b, size_t nb, uint32_t *out,
@@ -592,10 +601,15 @@ static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
   if (host) {
     if (len_dev_user) return ctx_fail(ctx, SETOPS_ERR_INVALID, "async call with host pointers");
     void *va = mn ? device_view(a) : nullptr, *vb = mn ? device_view(b) : nullptr;
-    if (va && vb && read_in_place(choice, mn, std::max<uint64_t>(na, nb))) {
+    if (va && vb && read_in_place(choice)) {
       da = static_cast<const uint32_t *>(va);
       db = static_cast<const uint32_t *>(vb);
-      if (choice.algo == ALGO_BITMAP && choice.variant == kStagedWindow) choice.variant = 0;
+      // a search over host memory waits on the link for every probe round:
+      // under the default policy the thread-per-element variant gives way to
+      // nine-way rounds with eight lanes per element (0.28 against 0.37 ms
+      // for 2^18 against 2^24 in place)
+      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && choice.variant == 0)
+        choice.variant = 3;
     } else if (mn > 0) {
       RK(ctx_stage_in(ctx, 0, a, na, &da));
       RK(ctx_stage_in(ctx, 1, b, nb, &db));
@@ -992,8 +1006,9 @@ static int svs_impl(setops_ctx *ctx, const uint32_t *const *sets,
       j.choice.algo = ALGO_GALLOP;
       int band = 0;
       while (band < kRatioBands - 1 && (1u << band) < thr) ++band;
-      j.choice.variant = int((ctx->policy[0][band] & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
-      if ((ctx->policy[0][band] & SETOPS_ALGO_MASK) != SETOPS_ALGO_GALLOP) j.choice.variant = 0;
+      const unsigned pol = ctx->policy[0][band][size_class(ub)];
+      j.choice.variant = int((pol & SETOPS_VARIANT_MASK) >> SETOPS_VARIANT_SHIFT);
+      if ((pol & SETOPS_ALGO_MASK) != SETOPS_ALGO_GALLOP) j.choice.variant = 0;
       RK(ctx_launch_pair(ctx, j));
     }
     ub = std::min(ub, nb);

@@ -15,6 +15,12 @@ namespace setops {
 constexpr int kSyncSlots = 8;      // coordination words (one per stream lane)
 constexpr int kLenWords = 64;      // device u64 result slots
 constexpr int kRatioBands = 32;    // policy bands: floor(log2(max/min))
+constexpr int kSizeClasses = 4;    // policy size classes of min(na, nb)
+// Size class of a pair by its smaller input: [0, 2^12), [2^12, 2^16),
+// [2^16, 2^22), [2^22, ...)
+inline int size_class(uint64_t mn) {
+  return mn < (uint64_t(1) << 12) ? 0 : mn < (uint64_t(1) << 16) ? 1 : mn < (uint64_t(1) << 22) ? 2 : 3;
+}
 constexpr uint64_t kMinTilesPerCta = 4;  // merge: tiles per CTA before more CTAs
 
 struct DevBuf {
@@ -68,8 +74,7 @@ struct setops_ctx {
   uint32_t epoch = 1;
   uint64_t launches = 0;
   std::map<const void *, int> occ;
-  unsigned policy[2][setops::kRatioBands] = {};
-  uint32_t policy_user[2] = {};  // bit b: band b was set by setops_gpu_set_policy
+  unsigned policy[2][setops::kRatioBands][setops::kSizeClasses] = {};
   int batch_variant = 0;             // batch kernel shape
   uint32_t batch_search_ratio = 16;  // batch pairs with max/min >= this: search path
 
