@@ -209,6 +209,18 @@ int setops_gpu_svs_count(setops_ctx *ctx, const uint32_t *const *sets,
 int setops_gpu_svs_async(setops_ctx *ctx, const uint32_t *const *sets,
                          const size_t *lens, size_t k, uint32_t *out,
                          size_t out_cap, uint64_t *len_dev, unsigned flags);
+/* k-set intersection by the small_adaptive scheme (the reference's
+ * small_adaptive, setops/src/intersect/adaptive.rs:107-148, an IntersectK,
+ * setops/src/intersect.rs:42): every element of the smallest set is looked
+ * up in the other sets, smallest first, and dropped at the first one that
+ * lacks it, so the larger sets are read only where the survivors lie.  Same
+ * arguments and result as setops_gpu_svs (out_cap >= the smallest length;
+ * SETOPS_HOST for host arrays); k <= 16. */
+int setops_gpu_adaptive(setops_ctx *ctx, const uint32_t *const *sets, const size_t *lens,
+                        size_t k, uint32_t *out, size_t out_cap, size_t *out_len,
+                        unsigned flags);
+int setops_gpu_adaptive_count(setops_ctx *ctx, const uint32_t *const *sets, const size_t *lens,
+                              size_t k, uint64_t *count, unsigned flags);
 
 /* ---- batched 2-set --------------------------------------------------------
  * Many independent pairs in one launch.  Replaces a loop of Intersect2 /

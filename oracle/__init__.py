@@ -90,6 +90,8 @@ def lib() -> C.CDLL:
         L.orc_run_svs_groups.argtypes = [sz, C.POINTER(vp), C.POINTER(sz),
                                          C.POINTER(sz), C.POINTER(vp),
                                          C.POINTER(C.c_uint64), C.c_int]
+        L.orc_small_adaptive.restype = sz
+        L.orc_small_adaptive.argtypes = [C.POINTER(vp), C.POINTER(sz), sz, vp]
         L.orc_run_bsr_pairs.restype = C.c_int
         L.orc_run_bsr_pairs.argtypes = [C.c_int, sz] + [C.POINTER(vp)] * 2 + [C.POINTER(sz)] + \
             [C.POINTER(vp)] * 2 + [C.POINTER(sz)] + [C.POINTER(vp)] * 2 + \
@@ -213,6 +215,18 @@ def svs_generic(sets) -> np.ndarray:
     n = lib().orc_svs_generic(ptrs, lens, k, left.ctypes.data, right.ctypes.data, C.byref(res))
     buf = left if res.value == left.ctypes.data else right
     return buf[:n].copy()
+
+
+def small_adaptive(sets) -> np.ndarray:
+    """small_adaptive (setops/src/intersect/adaptive.rs:107-148) over
+    [s0, s1, ...]; s0 is the set whose elements are looked up."""
+    arrs = [_u32(s) for s in sets]
+    k = len(arrs)
+    out = np.empty(max(arrs[0].size if arrs else 0, 1), np.uint32)
+    P = (C.c_void_p * k)(*[_ptr(a) for a in arrs])
+    N = (C.c_size_t * k)(*[a.size for a in arrs])
+    n = lib().orc_small_adaptive(P, N, k, out.ctypes.data)
+    return out[:n].copy()
 
 
 def run_pairs(algo: int, pairs, nthreads: int = 1, outs=None) -> np.ndarray:

@@ -251,6 +251,41 @@ size_t orc_svs_generic(const uint32_t *const *sets, const size_t *lens,
   return svs_with(orc_naive_merge, sets, lens, k, left, right, result);
 }
 
+/* small_adaptive (setops/src/intersect/adaptive.rs:107-148, Demaine,
+ * Lopez-Ortiz and Munro 2001): every element of sets[0] is looked up in each
+ * later set in turn, galloping from that set's last position (offset doubles
+ * while set[base + offset] <= element, then a binary search of [base,
+ * min(len - 1, base + offset)]); the first set that lacks it moves on to the
+ * next element; an element found in every set is emitted.  k <= 64. */
+size_t orc_small_adaptive(const uint32_t *const *sets, const size_t *lens, size_t k,
+                          uint32_t *out) {
+  if (k < 2 || k > 64) return 0;
+  size_t pos[64] = {0};
+  size_t n = 0;
+  for (size_t e = 0; e < lens[0]; e++) {
+    const uint32_t element = sets[0][e];
+    int found_all = 1;
+    for (size_t i = 1; i < k; i++) {
+      const uint32_t *set = sets[i];
+      const size_t len = lens[i];
+      const size_t base = pos[i];
+      size_t offset = 1;
+      while (base + offset < len && set[base + offset] <= element) offset *= 2;
+      const ptrdiff_t lo = (ptrdiff_t)base;
+      ptrdiff_t hi = (ptrdiff_t)len - 1;
+      if ((ptrdiff_t)(base + offset) < hi) hi = (ptrdiff_t)(base + offset);
+      const size_t nb = orc_binary_search(set, element, lo, hi);
+      pos[i] = nb;
+      if (nb >= len || set[nb] != element) {
+        found_all = 0;
+        break;
+      }
+    }
+    if (found_all) EMIT(out, n, element);
+  }
+  return n;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Portable SIMD restatements (GCC vector extensions).                      */
 

@@ -94,6 +94,10 @@ size_t orc_galloping_bsr(const uint32_t *ba, const uint32_t *sa, size_t na,
  * sets are intersected in the order given (the reference assumes
  * smallest-first).  *result receives whichever buffer holds the answer;
  * returns its length.  k >= 2. */
+/* small_adaptive: setops/src/intersect/adaptive.rs:107-148 (sets[0] the
+ * probe set; k <= 64).  Returns the count; out (optional) gets the elements. */
+size_t orc_small_adaptive(const uint32_t *const *sets, const size_t *lens, size_t k,
+                          uint32_t *out);
 size_t orc_svs_generic(const uint32_t *const *sets, const size_t *lens,
                        size_t k, uint32_t *left, uint32_t *right,
                        uint32_t **result);

@@ -39,7 +39,7 @@ __all__ = [
     "Counter", "VecWriter", "SliceWriter", "UnsafeWriter",
     "BsrVec", "BsrRef",
     "gpu_auto", "gpu_merge", "gpu_galloping", "gpu_auto_c", "gpu_bsr",
-    "gpu_svs", "intersect", "intersect_count",
+    "gpu_svs", "gpu_small_adaptive", "intersect", "intersect_count",
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
@@ -631,7 +631,7 @@ def _algo_of(fn) -> int:
     return _ALGO_OF.get(fn, ALGO_AUTO)
 
 
-def _svs(sets, out=None, count_only=False, algo=ALGO_AUTO, ctx=None):
+def _svs(sets, out=None, count_only=False, algo=ALGO_AUTO, ctx=None, adaptive=False):
     ctx = ctx or default_context()
     bufs = [_Buf(s) for s in sets]
     flags = _space(bufs) | algo
@@ -640,7 +640,8 @@ def _svs(sets, out=None, count_only=False, algo=ALGO_AUTO, ctx=None):
     lens = (C.c_size_t * k)(*[b.n for b in bufs])
     if count_only:
         c = C.c_uint64()
-        ctx.check(lib.setops_gpu_svs_count(ctx.handle, ptrs, lens, k, C.byref(c), flags))
+        fn = lib.setops_gpu_adaptive_count if adaptive else lib.setops_gpu_svs_count
+        ctx.check(fn(ctx.handle, ptrs, lens, k, C.byref(c), flags))
         return int(c.value)
     mn = min((b.n for b in bufs), default=0)
     device = not (flags & HOST)
@@ -649,8 +650,23 @@ def _svs(sets, out=None, count_only=False, algo=ALGO_AUTO, ctx=None):
     optr = _Buf(out).ptr if device else out.ctypes.data
     ocap = (out.numel() if device and hasattr(out, "numel") else len(out))
     n = C.c_size_t()
-    ctx.check(lib.setops_gpu_svs(ctx.handle, ptrs, lens, k, optr, ocap, C.byref(n), flags))
+    fn = lib.setops_gpu_adaptive if adaptive else lib.setops_gpu_svs
+    ctx.check(fn(ctx.handle, ptrs, lens, k, optr, ocap, C.byref(n), flags))
     return out, int(n.value)
+
+
+def gpu_small_adaptive(sets, visitor, *, ctx: Context | None = None) -> None:
+    """``IntersectK`` by the small_adaptive scheme
+    (setops/src/intersect/adaptive.rs:107-148): each element of the smallest
+    set looked up in the others, smallest first, dropped at the first set
+    that lacks it.  Same result as gpu_svs."""
+    if len(sets) < 2:
+        raise SetopsError(_lib.ERR_INVALID, "k-set intersection needs >= 2 sets")
+    if isinstance(visitor, Counter):
+        visitor._count += _svs(sets, count_only=True, ctx=ctx, adaptive=True)
+        return
+    out, n = _svs(sets, ctx=ctx, adaptive=True)
+    visitor._extend(_to_host(out, n))
 
 
 def gpu_svs(sets, visitor, *, ctx: Context | None = None) -> None:

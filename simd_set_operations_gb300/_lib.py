@@ -86,6 +86,8 @@ SIGNATURES = [
     ("setops_gpu_svs", C.c_int, [vp, C.POINTER(vp), szp, sz, vp, sz, szp, uint]),
     ("setops_gpu_svs_count", C.c_int, [vp, C.POINTER(vp), szp, sz, u64p, uint]),
     ("setops_gpu_svs_async", C.c_int, [vp, C.POINTER(vp), szp, sz, vp, sz, vp, uint]),
+    ("setops_gpu_adaptive", C.c_int, [vp, C.POINTER(vp), szp, sz, vp, sz, szp, uint]),
+    ("setops_gpu_adaptive_count", C.c_int, [vp, C.POINTER(vp), szp, sz, u64p, uint]),
     ("setops_gpu_validate_sorted", C.c_int, [vp, vp, sz, C.POINTER(C.c_int), uint]),
     ("setops_gpu_intersect_noalloc", C.c_int, [vp, sz, vp, sz, vp, sz, szp, vp]),
     ("setops_gpu_batch_intersect", C.c_int, [vp, vp, sz, vp, vp, vp, vp, sz, vp, sz, vp, vp, uint]),

@@ -185,3 +185,24 @@ def test_bsr_pair_runner_equals_single_calls(orc):
         words = orc.run_bsr_pairs(pairs, 3, outs=outs, algo=algo)
         for (wb, ws), (ob, os_), w in zip(want, outs, words):
             assert np.array_equal(ob[:int(w)], wb) and np.array_equal(os_[:int(w)], ws)
+
+
+def test_small_adaptive_equals_svs_generic(orc):
+    """small_adaptive and svs_generic give the same k-set intersection (the
+    reference's property tests hold every k-set algorithm to one answer)."""
+    rng = np.random.default_rng(55)
+    for k in (2, 3, 5, 8):
+        core = rng.choice(1 << 18, 200, replace=False).astype(np.uint32)
+        sets = []
+        for i in range(k):
+            extra = rng.choice(1 << 18, 20000 // (i + 1), replace=False).astype(np.uint32)
+            sets.append(np.unique(np.concatenate([core, extra])))
+        sets.sort(key=len)
+        assert np.array_equal(orc.small_adaptive(sets), orc.svs_generic(sets)), k
+    # edges: an empty set, disjoint sets, identical sets, values near 2^32
+    e = np.empty(0, np.uint32)
+    x = np.array([1, 5, 0xFFFFFFFF], np.uint32)
+    assert orc.small_adaptive([e, x]).size == 0
+    assert orc.small_adaptive([x, e, x]).size == 0
+    assert orc.small_adaptive([x, np.array([2, 6], np.uint32)]).size == 0
+    assert np.array_equal(orc.small_adaptive([x, x.copy(), x.copy()]), x)
