@@ -20,7 +20,7 @@ def group(rng, k, n0, grow, core, hi):
     c = rand_set(rng, core, hi)
     sets = []
     for i in range(k):
-        extra = rand_set(rng, int(n0 * grow ** i), hi)
+        extra = rand_set(rng, min(int(n0 * grow ** i), hi // 2), hi)
         sets.append(np.union1d(c, extra).astype(np.uint32))
     return sets
 
