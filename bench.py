@@ -74,6 +74,7 @@ def parse():
     p.add_argument("--bsr-pairs", type=int, default=10000,
                    help="pairs of the BSR subset of the batch leg")
     p.add_argument("--no-kset", action="store_true", help="skip the k-set leg")
+    p.add_argument("--kset-ks", default="3,5,8", help="k values of the k-set leg")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the hand-written policy table (no tuning before the sweep)")
     p.add_argument("--no-config0", action="store_true",
@@ -371,7 +372,7 @@ def read_peak():
 def read_traffic():
     """DRAM bytes per launch of the headline kernel from the committed ncu
     summary (profiles/), or None."""
-    f = ROOT / "profiles" / "window_2e24x2e24_ncu.md"
+    f = ROOT / "profiles" / "awindow_2e24x2e24_ncu.md"
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read_text())
@@ -948,12 +949,31 @@ def kset_leg(ctx, stream, ks=(3, 5, 8), with_cpu: bool = True) -> dict:
         if not np.array_equal(out[:int(n_out.value)].cpu().numpy().view(np.uint32), want):
             raise SystemExit(f"k={k}: GPU result differs from svs_generic")
         cpu = cpu_kset_baseline(sets, want.size) if with_cpu else None
+        # the small_adaptive path on the same sets (synchronous calls, like
+        # ms_per_synchronous_call of SvS)
+        n_ad = C.c_size_t()
+
+        def run_ad():
+            ctx.check(L.setops_gpu_adaptive(ctx.handle, ptrs, lens, k, out.data_ptr(),
+                                            out.numel(), C.byref(n_ad), 0))
+        run_ad()
+        if n_ad.value != want.size or not np.array_equal(
+                out[:want.size].cpu().numpy().view(np.uint32), want):
+            raise SystemExit(f"k={k}: small_adaptive differs from svs_generic")
+        e0.record(stream)
+        for _ in range(reps):
+            run_ad()
+        e1.record(stream)
+        e1.synchronize()
+        t_ad = e0.elapsed_time(e1) * 1e-3 / reps
         rows.append({"k": k, "sizes": [int(x.size) for x in sets], "out": int(n_out.value),
                      "ms": 1e3 * t_dev, "kset_per_s": 1.0 / t_dev,
                      "GBps_algorithmic": alg / t_dev / 1e9, "frac_of_peak": alg / t_dev / 1e9 / peak,
                      "ms_per_synchronous_call": 1e3 * t, "ms_graph_replay": 1e3 * t_graph,
                      "GBps_graph_replay": alg / t_graph / 1e9,
-                     "results_match_svs_generic": True, "cpu_baseline": cpu})
+                     "results_match_svs_generic": True,
+                     "small_adaptive_ms_per_synchronous_call": 1e3 * t_ad,
+                     "cpu_baseline": cpu})
     return {"workload": "k-set SvS: k in {3, 5, 8}, |S_i| = 2^22 / i, density 0.2, core 5 % of "
                         "the smallest set, u32, materialised, smallest first; inputs resident",
             "api": "setops_gpu_svs_async back to back, device pointers (ms); setops_gpu_svs, "
@@ -1339,7 +1359,8 @@ def run_gb300(args):
         batch["bsr_subset"] = batch_bsr_leg(ctx, stream, args.bsr_pairs)
     kset = None
     if rank == 0 and not args.no_kset:
-        kset = kset_leg(ctx, stream, with_cpu=not args.no_cpu_baseline)
+        kset = kset_leg(ctx, stream, ks=tuple(int(x) for x in args.kset_ks.split(",")),
+                        with_cpu=not args.no_cpu_baseline)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_leg(ctx, [int(x) for x in args.serve_rates.split(",")],
