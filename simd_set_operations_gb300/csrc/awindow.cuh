@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
   uint64_t staged = 0;  // materialise: matches staged so far
   uint32_t *dst = MAT ? p.stage + ca0 : nullptr;
   uint64_t b = 0;       // first B element not yet consumed
-  uint32_t wc = 0;      // windows so far (s_le slot)
+  uint32_t wc = 0;      // this window's s_le / s_wt slot (windows so far, mod 3)
 
   // window state: [b, we) with aligned words [qa, qe), head [b, ha), tail
   // [bodyend, we); vb holds the window's words once loaded
@@ -279,18 +279,18 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
       else run(in_tile);
       if (!MAT) cnt += uint32_t(__popc(hm));
       le = __reduce_add_sync(0xffffffffu, le);
-      if (lane == 0 && le) atomicAdd(&s_le[wc % 3], le);
+      if (lane == 0 && le) atomicAdd(&s_le[wc], le);
       if (MAT) {
         const uint32_t wt = __reduce_add_sync(0xffffffffu, uint32_t(__popc(hm)));
-        if (lane == 0) s_wt[wc % 3][warp] = wt;
+        if (lane == 0) s_wt[wc][warp] = wt;
       }
       __syncthreads();
-      const uint32_t used = s_le[wc % 3];
+      const uint32_t used = s_le[wc];
       if (MAT) {
         uint32_t before = 0, wtot = 0;
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-          const uint32_t x = s_wt[wc % 3][q];
+          const uint32_t x = s_wt[wc][q];
           before += (q < warp) ? x : 0u;
           wtot += x;
         }
@@ -304,12 +304,23 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
         }
         const uint32_t hb = hm & ((1u << (4 * UB)) - 1u);  // body matches, lane order
         const uint32_t c = uint32_t(__popc(hb));
-        uint32_t ex = 0, tot = 0;
+        // this lane's place among the warp's matches: one ballot when no lane
+        // has more than one (the usual case at low selectivity), else a scan
+        // of the counts' bit planes
+        uint32_t ex, tot;
+        const unsigned one = __ballot_sync(0xffffffffu, c != 0);
+        if (__ballot_sync(0xffffffffu, c > 1) == 0) {
+          ex = uint32_t(__popc(one & lt));
+          tot = uint32_t(__popc(one));
+        } else {
+          ex = 0;
+          tot = 0;
 #pragma unroll
-        for (int bit = 0; bit < 5; ++bit) {
-          const unsigned pl = __ballot_sync(0xffffffffu, (c >> bit) & 1u);
-          ex += uint32_t(__popc(pl & lt)) << bit;
-          tot += uint32_t(__popc(pl)) << bit;
+          for (int bit = 0; bit < 5; ++bit) {
+            const unsigned pl = __ballot_sync(0xffffffffu, (c >> bit) & 1u);
+            ex += uint32_t(__popc(pl & lt)) << bit;
+            tot += uint32_t(__popc(pl)) << bit;
+          }
         }
         {
           // bit j = 4u + k of hb is element k of the lane's word u, which
@@ -327,8 +338,8 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
         }
         staged += wtot;
       }
-      if (t == 0) s_le[(wc + 2) % 3] = 0;
-      ++wc;
+      if (t == 0) s_le[wc == 0 ? 2 : wc - 1] = 0;  // the slot two windows on
+      wc = (wc == 2) ? 0 : wc + 1;
       b += used;
       if (b < we) break;  // an element above alast: the tile is done
     }

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
   uint64_t staged = 0;  // materialise: matches staged so far
   uint32_t *dst = MAT ? p.stage + ca0 : nullptr;
   uint64_t b = 0;       // first B element not yet consumed
-  uint32_t wc = 0;      // windows so far (s_le slot)
+  uint32_t wc = 0;      // this window's s_le / s_wt slot (windows so far, mod 3)
 
   for (uint32_t k = 0; k < ntiles; ++k) {
     // ---- 1. the A tile ----
@@ -329,18 +329,18 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
       // one barrier per window: slot wc%3 sums this window; the slot of two
       // windows on is cleared (its last readers passed this barrier)
       le = __reduce_add_sync(0xffffffffu, le);
-      if (lane == 0 && le) atomicAdd(&s_le[wc % 3], le);
+      if (lane == 0 && le) atomicAdd(&s_le[wc], le);
       if (MAT) {
         const uint32_t wt = __reduce_add_sync(0xffffffffu, uint32_t(__popc(hm)));
-        if (lane == 0) s_wt[wc % 3][warp] = wt;
+        if (lane == 0) s_wt[wc][warp] = wt;
       }
       __syncthreads();
-      const uint32_t used = s_le[wc % 3];
+      const uint32_t used = s_le[wc];
       if (MAT) {
         uint32_t before = 0, wtot = 0;  // matches of the warps before this one; of all
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-          const uint32_t x = s_wt[wc % 3][q];
+          const uint32_t x = s_wt[wc][q];
           before += (q < warp) ? x : 0u;
           wtot += x;
         }
@@ -387,8 +387,8 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
         }
         staged += wtot;
       }
-      if (t == 0) s_le[(wc + 2) % 3] = 0;
-      ++wc;
+      if (t == 0) s_le[wc == 0 ? 2 : wc - 1] = 0;  // the slot two windows on
+      wc = (wc == 2) ? 0 : wc + 1;
       b += used;
       if (b < we) break;  // an element above alast: the tile is done
     }
