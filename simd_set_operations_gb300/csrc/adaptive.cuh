@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(NT) adaptive_kernel(const AdaptiveArgs p) {
       uint64_t lo = 0, hi = 0;
       if (nj > 0) {
         uint32_t key;
-        const uint64_t est0 = uint64_t(double(e0) / double(n0) * double(nj));
-        const uint64_t est1 = uint64_t(double(e1) / double(n0) * double(nj));
+        const uint64_t est0 = guess_scale(e0, n0, nj);
+        const uint64_t est1 = guess_scale(e1, n0, nj);
         lo = warp_lower_bound_guess(Sj, nj, S0 + e0, est0 < nj ? est0 : nj - 1, &key);
         hi = warp_lower_bound_guess(Sj, nj, S0 + e1 - 1, est1 < nj ? est1 : nj - 1, &key);
         hi = (hi < nj) ? hi + 1 : nj;  // include an element equal to the last value

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
   if (ntiles) prefetch(0);
   // warp 0: where the run starts reading B (as in window.cuh)
   if (ntiles && warp == 0) {
-    const uint64_t est = uint64_t(double(ca0) / double(na) * double(nb));
+    const uint64_t est = guess_scale(ca0, na, nb);
     const uint64_t r = warp_start_below(B, nb, A + ca0, est);
     if (lane == 0) s_b0 = r;
   }

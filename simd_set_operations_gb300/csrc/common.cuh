@@ -46,6 +46,15 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
+// floor(x / den * num) as an index guess, at most num (den > 0).  Single
+// precision: this GPU's double-precision rate is a small fraction of its
+// single-precision one, and every guess here is followed by an exact search,
+// so a few significant digits are enough.
+__device__ __forceinline__ uint64_t guess_scale(uint64_t x, uint64_t den, uint64_t num) {
+  const float g = float(x) / float(den) * float(num);
+  return g <= 0.0f ? 0 : (g >= float(num) ? num : uint64_t(g));
+}
+
 __device__ __forceinline__ void record_error(int *err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
@@ -421,7 +430,7 @@ __device__ __forceinline__ uint64_t warp_lower_bound_guess(const uint32_t *__res
       const uint64_t g2 =
           (blast <= bfirst || key <= bfirst)
               ? lo
-              : uint64_t(double(key - bfirst) / double(blast - bfirst) * double(n - 1));
+              : guess_scale(key - bfirst, blast - bfirst, n - 1);
       const int64_t gg = int64_t(g2);
       narrow([&](int k) { return gg + int64_t(k - 64) * S; });
     }

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
     const int warp = t >> 5;
     if (warp < 2) {
       const uint64_t i = warp == 0 ? s0 : s1 - 1;
-      const uint64_t est = uint64_t(double(i) / double(ns) * double(nl));
+      const uint64_t est = guess_scale(i, ns, nl);
       uint64_t lo, hi;
       warp_bracket_guess(L, nl, S + i, est, &lo, &hi);
       if (lane == 0) s_br[warp] = warp == 0 ? lo : hi;

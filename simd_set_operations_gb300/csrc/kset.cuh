@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(NT, MINB) kset_kernel(const KsetArgs p) {
       auto guess = [&](uint32_t v) -> uint64_t {
         return (blast <= bfirst || v <= bfirst)
                    ? 0
-                   : uint64_t(double(v - bfirst) / double(blast - bfirst) * double(nb - 1));
+                   : guess_scale(v - bfirst, blast - bfirst, nb - 1);
       };
       const uint64_t est = guess(key);
       if (lane == 0) {

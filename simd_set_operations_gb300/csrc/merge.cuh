@@ -201,7 +201,7 @@ __device__ __forceinline__ uint64_t corank_search(const uint32_t *A,
       s_hi = hi;
     }
     __syncthreads();
-    uint64_t est = uint64_t(double(d) * double(na) / double(na + nb));
+    uint64_t est = guess_scale(d, na + nb, na);
     if (est < lo) est = lo;
     if (est >= hi) est = hi - 1;
     // probes est + (2^k - 1) and est - 2^k, k = 0..47

@@ -203,7 +203,7 @@ __device__ __forceinline__ uint64_t tile_run(const uint32_t *A, uint64_t i_begin
   const uint32_t blast = (search && nb) ? __ldg(B + nb - 1) : 0u;
   auto guess = [&](uint32_t key) -> uint64_t {
     if (blast <= bfirst || key <= bfirst) return 0;
-    return uint64_t(double(key - bfirst) / double(blast - bfirst) * double(nb - 1));
+    return guess_scale(key - bfirst, blast - bfirst, nb - 1);
   };
   uint32_t cnt = 0;       // count mode
   uint64_t staged = 0;    // materialise: matches written so far

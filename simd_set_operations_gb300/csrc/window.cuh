@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(NT, MINB) window_kernel(const MergeArgs p) {
   // nothing in this run), from a guess at the same fraction of B as ca0 is
   // of A
   if (ntiles && warp == 0) {
-    const uint64_t est = uint64_t(double(ca0) / double(na) * double(nb));
+    const uint64_t est = guess_scale(ca0, na, nb);
     const uint64_t r = warp_start_below(B, nb, A + ca0, est);
     if (lane == 0) s_b0 = r;
   }

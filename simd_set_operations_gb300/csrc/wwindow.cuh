@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(NT, MINB) wwindow_kernel(const MergeArgs p) {
     // run), from a guess at the same fraction of B as ra0 is of A ----
     uint64_t qb;
     {
-      const uint64_t est = uint64_t(double(ra0) / double(na) * double(nb));
+      const uint64_t est = guess_scale(ra0, na, nb);
       qb = (bmis + warp_start_below(B, nb, A + ra0, est)) >> 2;
     }
 
