@@ -382,12 +382,21 @@ __global__ void __launch_bounds__(NT, MINB) awindow_kernel(const MergeArgs p) {
   if constexpr (MAT) {
     if (t == 0) p.coranks[blockIdx.x] = staged;
     if (!grid_barrier(&p.sync->done, G, p.err)) return;
+    // counts of CTAs 0..c-1 (plain loads: every CTA published before the
+    // barrier): a thread's loads all issued at once, one round trip, for up
+    // to 16 * NT CTAs; a larger grid adds a loop for the rest
     uint64_t before = 0;
     {
-      uint32_t c = uint32_t(t);
-      for (; c + 3 * NT < blockIdx.x; c += 4 * NT)
-        before += (p.coranks[c] + p.coranks[c + NT]) + (p.coranks[c + 2 * NT] + p.coranks[c + 3 * NT]);
-      for (; c < blockIdx.x; c += NT) before += p.coranks[c];
+      constexpr int PL = 16;
+      uint64_t w[PL];
+#pragma unroll
+      for (int j = 0; j < PL; ++j) {
+        const uint32_t c = uint32_t(t + j * NT);
+        w[j] = c < blockIdx.x ? p.coranks[c] : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < PL; ++j) before += w[j];
+      for (uint32_t c = uint32_t(t + PL * NT); c < blockIdx.x; c += NT) before += p.coranks[c];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
