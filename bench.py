@@ -10,7 +10,8 @@ pair is intersected exactly (materialised, ascending) with the algorithm the
 policy picks for its size ratio.
 
 * ``value``: pair intersections/s with inputs resident in HBM (device
-  pointers, async C-ABI calls), timed with CUDA events over K steps.
+  pointers, async C-ABI calls; the K steps captured once into a CUDA graph,
+  the steady-state form), timed with CUDA events over one replay.
 * ``e2e``: the same through the host-pointer C-ABI call
   (``setops_gpu_intersect(..., SETOPS_HOST)``): pinned host inputs copied in
   and the result copied out inside the timed region.
@@ -75,6 +76,8 @@ def parse():
                    help="pairs of the BSR subset of the batch leg")
     p.add_argument("--no-kset", action="store_true", help="skip the k-set leg")
     p.add_argument("--kset-ks", default="3,5,8", help="k values of the k-set leg")
+    p.add_argument("--no-graph", action="store_true",
+                   help="time the sweep's calls directly instead of one CUDA-graph replay")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the hand-written policy table (no tuning before the sweep)")
     p.add_argument("--no-config0", action="store_true",
@@ -1182,15 +1185,17 @@ def run_gb300(args):
         if rc != 0:
             ctx.check(rc)
 
-    def step(ev=None):
+    def step(ev=None, rec=None):
         # ev: an event pair around the headline launch (every event recorded
-        # between launches costs device time, so only that one is bracketed)
+        # between launches costs device time, so only that one is bracketed);
+        # rec: how to record an event (inside a graph capture: an external
+        # record, so that the event times every replay)
         for i in range(len(pairs)):
             if ev is not None and i == head:
-                ev[0].record(stream)
+                rec(ev[0]) if rec else ev[0].record(stream)
             launch(i)
             if ev is not None and i == head:
-                ev[1].record(stream)
+                rec(ev[1]) if rec else ev[1].record(stream)
 
     def barrier():
         if world > 1:
@@ -1221,17 +1226,47 @@ def run_gb300(args):
     def mk():
         return torch.cuda.Event(enable_timing=True)
     evs = [(mk(), mk()) for _ in range(args.steps)]
+    for e0, e1 in evs:  # creates the events before any capture
+        e0.record(stream)
+        e1.record(stream)
+    graph = None
+    launches0 = ctx.launch_count
+    if not args.no_graph:
+        # the K steps captured once into a CUDA graph (the library's
+        # asynchronous calls: the steady-state form of a repeated workload);
+        # one replay is the timed region
+        def rec(e):
+            ctx.check(L.setops_bench_record_event(C.c_void_p(e.cuda_event),
+                                                  C.c_void_p(stream.cuda_stream)))
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            for k in range(args.steps):
+                step(evs[k], rec)
+        launches = ctx.launch_count - launches0
+        graph.replay()  # untimed
+    torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    launches0 = ctx.launch_count
     t_start, t_end = mk(), mk()
     t_start.record(stream)
-    for k in range(args.steps):
-        step(evs[k])
+    if graph is not None:
+        graph.replay()
+    else:
+        for k in range(args.steps):
+            step(evs[k])
     t_end.record(stream)
     torch.cuda.synchronize()
     barrier()
-    launches = ctx.launch_count - launches0
+    if graph is None:
+        launches = ctx.launch_count - launches0
+    # the same K steps as plain calls, for comparison (no events inside)
+    p0, p1 = mk(), mk()
+    p0.record(stream)
+    for k in range(args.steps):
+        step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / args.steps
     clocks = sampler.stop()
     head_times = [e0.elapsed_time(e1) for e0, e1 in evs]
     wall_ms = t_start.elapsed_time(t_end)
@@ -1379,10 +1414,15 @@ def run_gb300(args):
         "config0": config0,
         "batch": batch, "kset": kset, "serve": serve,
         "timing": {"bracket_ms_total": wall_ms, "headline_ms_total": sum(head_times),
-                   "note": "value = pairs / CUDA-event time of the K-step bracket (no host "
-                           "sync inside; one event pair per step around the headline "
-                           "launch); sweep[].ms_back_to_back: each pair launched 20 times "
-                           "back to back after the timed region"},
+                   "cuda_graph": graph is not None,
+                   "plain_calls_ms_per_step": plain_ms,
+                   "note": "value = pairs / CUDA-event time of the K-step bracket: one replay "
+                           "of a CUDA graph holding the K steps' asynchronous library calls "
+                           "(--no-graph: the calls themselves), one event pair per step "
+                           "around the headline launch (external event records inside the "
+                           "graph); plain_calls_ms_per_step: the same K steps as plain calls "
+                           "after it; sweep[].ms_back_to_back: each pair launched 20 times "
+                           "back to back"},
     }
     if rank == 0:
         print(json.dumps(line))

@@ -142,6 +142,12 @@ int setops_bench_bsr_pairs_one_by_one(struct setops_ctx *ctx, const uint32_t *ba
  * offs and lens are host arrays), the answer to the device buffer out
  * (capacity out_cap, reused by every query).  latency_ns[q] (optional) gets
  * the call's wall time and counts[q] (optional) its answer's length. */
+/* cudaEventRecordWithFlags(event, stream, cudaEventRecordExternal): an event
+ * record that, made while `stream` is being captured into a CUDA graph,
+ * records `event` at that point of every replay (so a captured region can be
+ * timed).  Outside a capture it is a plain record.  Exported by
+ * libsetops_gpu.so; event and stream are a cudaEvent_t and a cudaStream_t. */
+int setops_bench_record_event(void *event, void *stream);
 int setops_bench_queries_one_by_one(struct setops_ctx *ctx, const uint32_t *pool,
                                     const uint64_t *offs, const uint64_t *lens,
                                     const uint32_t *ids, const uint32_t *ks, size_t kstride,

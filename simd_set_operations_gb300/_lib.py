@@ -114,6 +114,7 @@ SIGNATURES = [
                                                 C.POINTER(C.c_double)]),
     ("setops_bench_bsr_pairs_one_by_one", C.c_int, [vp, vp, vp, vp, vp, vp, vp, sz, vp, vp, vp,
                                                     vp, C.POINTER(C.c_double)]),
+    ("setops_bench_record_event", C.c_int, [vp, vp]),
     ("setops_bench_queries_one_by_one", C.c_int, [vp, vp, vp, vp, vp, vp, sz, sz, vp, sz, vp,
                                                   vp, C.POINTER(C.c_double)]),
 ]

@@ -3,6 +3,8 @@
 // pair, one k-set call per query, looped in C++ so that the baselines of the
 // batched and served paths are timed without foreign-language call overhead.
 #include <chrono>
+
+#include <cuda_runtime.h>
 #include <vector>
 
 #include "../../include/setops_bench.h"
@@ -62,6 +64,14 @@ int setops_bench_bsr_pairs_one_by_one(setops_ctx *ctx, const uint32_t *bases,
   }
   if (seconds) *seconds = now_s() - t0;
   return SETOPS_OK;
+}
+
+int setops_bench_record_event(void *event, void *stream) {
+  if (!event) return SETOPS_ERR_INVALID;
+  const cudaError_t e = cudaEventRecordWithFlags(static_cast<cudaEvent_t>(event),
+                                                 static_cast<cudaStream_t>(stream),
+                                                 cudaEventRecordExternal);
+  return e == cudaSuccess ? SETOPS_OK : SETOPS_ERR_CUDA;
 }
 
 int setops_bench_queries_one_by_one(setops_ctx *ctx, const uint32_t *pool, const uint64_t *offs,
