@@ -18,7 +18,7 @@ The reference's pieces and what stands in for them here:
   ``gpu_galloping``, ``gpu_bitmap``, ``gpu_bitmap_coarse`` (the tiled bitmap
   kernel with coarse bitmaps for sparse tiles) (2-set; on k-set data:
   smallest-first SvS with that kernel), ``gpu_svs`` (k-set, automatic),
-  ``gpu_bsr`` (BSR
+  ``gpu_small_adaptive`` (k-set, small_adaptive), ``gpu_bsr`` (BSR
   2-set; encoding outside the timed region, as the reference's harness,
   benchmark/src/timer/harness.rs:121-122).  Names of the reference's CPU
   algorithms are reported as unknown, as the reference does for names it
@@ -258,6 +258,33 @@ def _bsr_timer(ctx, sets, count_only, warmup_s):
     return _timed(ctx, call, warmup_s)
 
 
+def _adaptive_timer(ctx, sets, count_only, warmup_s):
+    """small_adaptive (setops/src/intersect/adaptive.rs:107-148) on the GPU:
+    each call waits for its result length (the k-set entry point is
+    synchronous)."""
+    import torch
+
+    from ._lib import lib
+    if len(sets) < 2:
+        raise ValueError("gpu_small_adaptive takes k-set data")
+    dsets = [torch.from_numpy(np.ascontiguousarray(s).view(np.int32)).cuda() for s in sets]
+    k = len(sets)
+    ptrs = (C.c_void_p * k)(*[d.data_ptr() for d in dsets])
+    lens = (C.c_size_t * k)(*[int(s.size) for s in sets])
+    cap = min(int(s.size) for s in sets)
+    out = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    n = C.c_size_t()
+    cnt = C.c_uint64()
+
+    def call():
+        if count_only:
+            ctx.check(lib.setops_gpu_adaptive_count(ctx.handle, ptrs, lens, k, C.byref(cnt), 0))
+        else:
+            ctx.check(lib.setops_gpu_adaptive(ctx.handle, ptrs, lens, k, out.data_ptr(), cap,
+                                              C.byref(n), 0))
+    return _timed(ctx, call, warmup_s)
+
+
 # SETOPS_ALGO_BITMAP variant with coarse bitmaps for sparse tiles
 BITMAP_COARSE_VARIANT = 7
 
@@ -273,11 +300,12 @@ def _registry() -> dict[str, Timer]:
                                    _pair_timer(ALGO_BITMAP | VARIANT(BITMAP_COARSE_VARIANT))),
         "gpu_svs": Timer("gpu_svs", _svs_timer(None)),
         "gpu_bsr": Timer("gpu_bsr", _bsr_timer),
+        "gpu_small_adaptive": Timer("gpu_small_adaptive", _adaptive_timer),
     }
 
 
 TIMER_NAMES = ("gpu_auto", "gpu_merge", "gpu_galloping", "gpu_bitmap", "gpu_bitmap_coarse",
-               "gpu_svs", "gpu_bsr")
+               "gpu_svs", "gpu_bsr", "gpu_small_adaptive")
 
 
 def timer(name: str) -> Timer | None:

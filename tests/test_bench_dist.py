@@ -62,3 +62,21 @@ def test_single_process_defaults(monkeypatch):
     assert bench.dist_env() == (0, 1, 0)
     assert bench.max_over_ranks(2.0) == 2.0
     assert bench.job_value(1, 4, 10, 2.0) == 20.0
+
+
+def test_touched_bytes_and_summary():
+    """The bench's estimate of the bytes a search-band pair touches (the
+    sectors its probes reach, capped at the whole larger set) and the
+    summary object built from the legs (absent legs give no keys)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    ns, nl = 1 << 10, 1 << 24
+    per = 14 - 2  # ceil(log2(2^14)) - 2 sectors per small element
+    assert bench.touched_bytes(ns, nl, 10) == 4 * ns + 40 + 32 * per * ns
+    assert bench.touched_bytes(1 << 22, nl, 0) == 4 * (1 << 22) + 4 * nl  # capped
+    sizes = [bench.touched_bytes(1 << e, nl, 0) for e in range(4, 20)]
+    assert sizes == sorted(sizes)
+    assert bench.algorithmic_bytes(1 << 24, 1 << 24, 167_772) == 134_888_816
+    s = bench.summarize({"frac": 0.4123}, None, None, None, None, None, None)
+    assert s == {"headline_frac": 0.412, "sweep_e2e_pairs_per_s": None,
+                 "sweep_cpu_pairs_per_s": None}

@@ -134,7 +134,11 @@ def test_registered_timers_run(small, ctx):
     exp, root = small
     ex.generate(exp, root)
     exp["algorithm_sets"]["two"] = list(ex.TIMER_NAMES[:5]) + ["gpu_bsr"]
+    for e in exp["experiment"]:
+        if e.get("algorithms") == ["gpu_svs"]:
+            e["algorithms"] = ["gpu_svs", "gpu_small_adaptive"]
     res = ex.run(exp, root, ctx=ctx, warmup_s=0.0, log=lambda m: None)
+    assert res["datasets"]["dk"]["algos"]["gpu_small_adaptive"], "k-set timer did not run"
     for d in res["datasets"].values():
         for name, runs in d["algos"].items():
             assert runs and all(t > 0 for r in runs for t in r["times"]), name
