@@ -182,7 +182,7 @@ int batch_impl(setops_ctx *ctx, const uint32_t *pool, size_t pool_len, const uin
 
 // ---- BSR pairs ----
 constexpr int kBsrThreads = 256;
-constexpr int kBsrCapWords = 2048;  // longer set staged in shared memory up to this many words
+constexpr int kBsrCapWords = 4096;  // longer set staged in shared memory up to this many words
 
 int launch_batch_bsr(setops_ctx *ctx, const BatchBsrArgs &a0, bool mat) {
   const void *fn = mat ? reinterpret_cast<const void *>(&batch_bsr_kernel<kBsrThreads, kBsrCapWords, true>)
