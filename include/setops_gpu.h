@@ -61,7 +61,11 @@ enum {
 #define SETOPS_ALGO_GALLOP (2u << SETOPS_ALGO_SHIFT) /* search kernel        */
 #define SETOPS_ALGO_BITMAP (3u << SETOPS_ALGO_SHIFT) /* tiled bitmap kernel  */
 /* Variant of the chosen kernel (tile shape / probe group); 0 = default.
- * setops_gpu_num_variants() gives the count per algorithm. */
+ * setops_gpu_num_variants() gives the count per algorithm.  For BSR sets,
+ * SETOPS_ALGO_MERGE variant 3 is the block-broadcast kernel (32-word blocks
+ * compared all against all, the scheme of broadcast_*_bsr,
+ * setops/src/intersect/broadcast.rs:163-357); it is the BSR default for
+ * size ratios below 32. */
 #define SETOPS_VARIANT_SHIFT 16
 #define SETOPS_VARIANT_MASK (0xffu << SETOPS_VARIANT_SHIFT)
 #define SETOPS_VARIANT(v) (((unsigned)(v) & 0xffu) << SETOPS_VARIANT_SHIFT)

@@ -7,6 +7,7 @@
 #include "tile.cuh"
 #include "window.cuh"
 #include "awindow.cuh"
+#include "bcast.cuh"
 #include "wwindow.cuh"
 #include "kset.cuh"
 
@@ -43,6 +44,13 @@ KernelInfo mk_awindow(const char *name) {
   using Cfg = AWindowCfg<NT, UA, UB, VW, MAT>;
   return KernelInfo{reinterpret_cast<const void *>(&awindow_kernel<NT, UA, UB, VW, MINB, MAT>),
                     NT, Cfg::kSmemBytes, Cfg::kTile, name, MAT};
+}
+
+template <int NT, int MINB, int KD, bool MAT>
+KernelInfo mk_bcast(const char *name) {
+  // materialise: cooperative (one grid barrier before the runs are placed)
+  return KernelInfo{reinterpret_cast<const void *>(&bcast_bsr_kernel<NT, MINB, KD, MAT>), NT, 0,
+                    BcastCfg<NT>::kTile, name, MAT};
 }
 
 template <int NT, int UA, int UB, int VWW, int MINB, bool MAT>
@@ -83,6 +91,8 @@ const KernelInfo kMergeBsr[][2] = {
     MERGE_ROW(8, 1024, 2, 3, 2048, true),  // 0: 56 KB
     MERGE_ROW(8, 2048, 2, 2, 4096, true),  // 1: 96 KB
     MERGE_ROW(8, 1024, 2, 2, 4096, true),  // 2: 64 KB
+    {mk_bcast<128, 8, 3, false>("bcast_bsr_128_k3"), mk_bcast<128, 8, 3, true>("bcast_bsr_128_k3")},
+    // 3: block broadcast, a warp per run of 32-word blocks (bcast.cuh)
 };
 // Window kernels: NT threads; UA / UB 16-byte loads per thread for an A tile
 // (4*UA*NT elements) / a B window (4*UB*NT); T of VW words (dense tiles span

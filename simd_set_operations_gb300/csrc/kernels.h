@@ -34,6 +34,9 @@ constexpr int kCoarseBitmap = 7;
 // SETOPS_ALGO_BITMAP variant whose materialise kernel stages both inputs in
 // shared memory by asynchronous copies (the default for size ratios below 2)
 constexpr int kStagedWindow = 8;
+// BSR SETOPS_ALGO_MERGE variant that compares 32-word blocks of the two sets
+// all against all, a warp per run of blocks (bcast.cuh)
+constexpr int kBcastBsr = 3;
 // The fused k-set kernel (kset.cuh): count or materialise.
 const KernelInfo &kset_kernel(bool mat);
 constexpr int kKsetThreads = 128;

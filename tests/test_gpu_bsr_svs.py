@@ -58,6 +58,34 @@ def test_bsr_random(ctx, orc, seed):
         check_bsr(ctx, orc, a, b)
 
 
+def _bsr_decode(bases, states):
+    """The sorted set whose BSR words these are (BsrVec::to_sorted_set)."""
+    bits = np.unpackbits(states.astype('<u4').view(np.uint8).reshape(-1, 4), axis=1,
+                         bitorder='little')
+    rows, cols = np.nonzero(bits)
+    return (bases[rows].astype(np.uint64) * 32 + cols).astype(np.uint32)
+
+
+@pytest.mark.parametrize("nw", [1, 31, 32, 33, 63, 64, 65, 1023, 1025, 4097, 70_001])
+def test_bsr_block_boundaries(ctx, orc, nw):
+    """Word counts around the 32-word blocks of the block-broadcast kernel
+    (and the merge kernels' chunks); half of the shared bases carry states
+    whose AND is zero, so those words are dropped."""
+    rng = np.random.default_rng(nw)
+    ab = np.arange(nw, dtype=np.uint32) * 2
+    ast = rng.integers(1, 2**32, size=nw, dtype=np.uint64).astype(np.uint32)
+    nbw = 2 * nw + 5
+    bbase = np.arange(nbw, dtype=np.uint32)
+    bst = rng.integers(1, 2**32, size=nbw, dtype=np.uint64).astype(np.uint32)
+    shared = np.arange(0, 2 * nw, 2)
+    zero = shared[rng.random(shared.size) < 0.5]
+    bst[zero] = ~ast[zero // 2]
+    bst[bst == 0] = 1
+    a, b = _bsr_decode(ab, ast), _bsr_decode(bbase, bst)
+    check_bsr(ctx, orc, a, b)
+    check_bsr(ctx, orc, b, a)
+
+
 def test_bsr_skewed(ctx, orc):
     rng = np.random.default_rng(11)
     s, l = ds.gen_twoset(11, 0.5, 0.1, 2000, 1 << 20)

@@ -216,8 +216,8 @@ def test_default_policy_bands(ctx, orc):
     window kernel with staged inputs (8) below ratio 2, its coarse-bitmap
     variant (7) for 2-31, then
     the search kernel (sampled, 8-lane, warp per element); BSR pairs take the
-    merge path below 32.  Each band's choice gives the oracle's result on a
-    pair of that ratio."""
+    block-broadcast variant of the merge family (3) below 32.  Each band's
+    choice gives the oracle's result on a pair of that ratio."""
     def algo_var(flags):
         return flags & 0xFF00, (flags >> 16) & 0xFF  # (algorithm bits, variant)
     want_arr = {0: (so.ALGO_BITMAP, 8), 1: (so.ALGO_BITMAP, 7), 4: (so.ALGO_BITMAP, 7),
@@ -227,7 +227,7 @@ def test_default_policy_bands(ctx, orc):
         got = algo_var(ctx.get_policy(False, band))
         assert got == (algo, var), (band, got)
     for band in (0, 4):
-        assert algo_var(ctx.get_policy(True, band))[0] == so.ALGO_MERGE
+        assert algo_var(ctx.get_policy(True, band)) == (so.ALGO_MERGE, 3)
     rng = np.random.default_rng(21)
     for ratio in (1, 2, 3, 5, 16, 31, 32, 600, 9000):
         na = 2000 if ratio < 600 else 200
