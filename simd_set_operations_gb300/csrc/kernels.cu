@@ -153,12 +153,12 @@ constexpr int count_of(const T (&)[N]) {
 // of 4096 words (dense tiles span < 131,072 values), 6 CTAs/SM
 const KernelInfo &kset_kernel(bool mat) {
   static const KernelInfo k[2] = {
-      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 5, 4096, 6, false>),
-                 kKsetThreads, KsetCfg<kKsetThreads, 4, 5, 4096, false>::kSmemBytes,
-                 KsetCfg<kKsetThreads, 4, 5, 4096, false>::kTile, "kset_count"},
-      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 5, 4096, 6, true>),
-                 kKsetThreads, KsetCfg<kKsetThreads, 4, 5, 4096, true>::kSmemBytes,
-                 KsetCfg<kKsetThreads, 4, 5, 4096, true>::kTile, "kset_mat", true}};
+      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 4, 4096, 3, false>),
+                 kKsetThreads, KsetCfg<kKsetThreads, 4, 4, 4096, false>::kSmemBytes,
+                 KsetCfg<kKsetThreads, 4, 4, 4096, false>::kTile, "kset_count"},
+      KernelInfo{reinterpret_cast<const void *>(&kset_kernel<kKsetThreads, 4, 4, 4096, 3, true>),
+                 kKsetThreads, KsetCfg<kKsetThreads, 4, 4, 4096, true>::kSmemBytes,
+                 KsetCfg<kKsetThreads, 4, 4, 4096, true>::kTile, "kset_mat", true}};
   return k[mat ? 1 : 0];
 }
 

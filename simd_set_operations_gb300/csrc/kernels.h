@@ -39,7 +39,11 @@ constexpr int kStagedWindow = 8;
 constexpr int kBcastBsr = 3;
 // The fused k-set kernel (kset.cuh): count or materialise.
 const KernelInfo &kset_kernel(bool mat);
-constexpr int kKsetThreads = 128;
+// 256 threads, 4096-element tiles of the smallest set, 3 CTAs per SM: of 16
+// shapes timed on the k-set configuration (k = 3, 5, 8) the fastest in sum,
+// 22.9 / 27.7 / 35.1 us against 24.3 / 31.3 / 40.3 for 128 threads with
+// 2048-element tiles at 6 CTAs per SM
+constexpr int kKsetThreads = 256;
 // kind: 0 count, 1 materialise
 const KernelInfo &variant(Algo algo, bool bsr, bool mat, int v);
 
