@@ -1094,6 +1094,7 @@ def summarize(roofline, e2e, cpu, config0, batch, kset, serve) -> dict:
     r = lambda x, n=3: None if x is None else round(float(x), n)  # noqa: E731
     out = {"headline_frac": r(g(roofline, "frac")),
            "sweep_e2e_pairs_per_s": r(g(e2e, "value"), 1),
+           "sweep_e2e_per_call_pairs_per_s": r(g(e2e, "per_call", "value"), 1),
            "sweep_cpu_pairs_per_s": r(g(cpu, "value"), 1)}
     if config0:
         out["config0"] = {"pairs_per_s": r(config0["pairs_per_s"], 1),
@@ -1337,17 +1338,43 @@ def run_gb300(args):
                 tot_out += n_out.value
             return tot_out
 
+        # the whole step in one call: setops_gpu_intersect_pairs overlaps the
+        # balanced pair's input copy with the in-place searches
+        npr = len(pinned)
+        P, S = C.c_void_p * npr, C.c_size_t * npr
+        outs2 = [torch.empty(ps.size, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+                 for ps, _, _ in pinned]
+        arr_a, arr_la = P(*[ps.ctypes.data for ps, _, _ in pinned]), S(*[ps.size for ps, _, _ in pinned])
+        arr_b, arr_lb = P(*[pl.ctypes.data for _, pl, _ in pinned]), S(*[pl.size for _, pl, _ in pinned])
+        arr_o, arr_co = P(*[o.ctypes.data for o in outs2]), S(*[o.size for o in outs2])
+        arr_len = S()
+
+        def step_e2e_pairs():
+            rc = L.setops_gpu_intersect_pairs(h, npr, arr_a, arr_la, arr_b, arr_lb, arr_o, arr_co,
+                                              arr_len, _lib.HOST)
+            if rc != 0:
+                ctx.check(rc)
+            return sum(int(x) for x in arr_len)
+
+        def timed(fn, steps):
+            barrier()
+            t0 = time.perf_counter()
+            tot = 0
+            for _ in range(steps):
+                tot = fn()
+            el = time.perf_counter() - t0
+            barrier()
+            return max_over_ranks(el), tot
+
         for _ in range(max(2, args.warmup // 2)):
             step_e2e()
+            step_e2e_pairs()
         e2e_steps = max(3, min(args.steps, 20))
-        barrier()
-        t0 = time.perf_counter()
-        tot_out = 0
-        for _ in range(e2e_steps):
-            tot_out = step_e2e()
-        e_el = time.perf_counter() - t0
-        barrier()
-        e_el = max_over_ranks(e_el)
+        pc_el, tot_out = timed(step_e2e, e2e_steps)
+        e_el, tot_out2 = timed(step_e2e_pairs, e2e_steps)
+        same = tot_out2 == tot_out and all(
+            int(arr_len[i]) <= po.size and np.array_equal(outs2[i][:int(arr_len[i])], po[:int(arr_len[i])])
+            for i, (_, _, po) in enumerate(pinned))
         h2d = sum(4 * (s.size + l.size) for s, l in pairs)
         d2h = 4 * tot_out + 8 * len(pairs)
         # what crosses the host link: a search-band pair is read in place and
@@ -1360,9 +1387,15 @@ def run_gb300(args):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "ms_per_step": 1e3 * e_el / e2e_steps,
                "h2d_bytes_moved_est": moved,
-               "api": "setops_gpu_intersect(..., SETOPS_HOST) from pinned host buffers: "
-                      "search-band pairs are read in place over the host link (NVLink-C2C), "
-                      "balanced pairs copied first; results written into the pinned output"}
+               "api": "setops_gpu_intersect_pairs(..., SETOPS_HOST), one call per step from "
+                      "pinned host buffers: the search-band pairs are read in place over the host "
+                      "link (NVLink-C2C) on a second stream while the balanced pair's inputs are "
+                      "copied; results written into the pinned outputs",
+               "results_match_per_call": bool(same),
+               "per_call": {"value": job_value(world, len(pairs), e2e_steps, pc_el), "unit": UNIT,
+                            "ms_per_step": 1e3 * pc_el / e2e_steps,
+                            "api": "setops_gpu_intersect(..., SETOPS_HOST), one call per pair, "
+                                   "the same buffers: each pair's copies and kernel in turn"}}
 
     # CPU baseline (rank 0 at N=1 only), also the cross-check of the results
     cpu = None

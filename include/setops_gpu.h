@@ -162,6 +162,20 @@ int setops_gpu_intersect_async(setops_ctx *ctx, const uint32_t *a, size_t na,
                                const uint32_t *b, size_t nb, uint32_t *out,
                                size_t out_cap, uint64_t *len_dev,
                                unsigned flags);
+/* npairs independent pairs in host memory (flags must include SETOPS_HOST):
+ * pair i is a[i] (na[i] elements) and b[i] (nb[i]); its result goes to
+ * out[i] (out_cap[i] >= min(na[i], nb[i])) and its length to out_len[i] --
+ * for every pair exactly what setops_gpu_intersect gives.  The reference has
+ * one Intersect2C call per pair (setops/src/intersect.rs:41); one call for
+ * many lets the search-band pairs with pinned inputs and outputs, read in
+ * place, run while the other pairs' inputs are copied over the host link.
+ * Synchronous; pairs with a pageable output are intersected one call each
+ * after the rest. */
+int setops_gpu_intersect_pairs(setops_ctx *ctx, size_t npairs,
+                               const uint32_t *const *a, const size_t *na,
+                               const uint32_t *const *b, const size_t *nb,
+                               uint32_t *const *out, const size_t *out_cap,
+                               size_t *out_len, unsigned flags);
 
 /* ---- 2-set, BSR (base-and-state) -----------------------------------------
  * Replace `Intersect2Bsr = fn(BsrRef, BsrRef, &mut BsrVec)`

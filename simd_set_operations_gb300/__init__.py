@@ -39,7 +39,7 @@ __all__ = [
     "Counter", "VecWriter", "SliceWriter", "UnsafeWriter",
     "BsrVec", "BsrRef",
     "gpu_auto", "gpu_merge", "gpu_galloping", "gpu_auto_c", "gpu_bsr",
-    "gpu_svs", "gpu_small_adaptive", "intersect", "intersect_count",
+    "gpu_svs", "gpu_small_adaptive", "intersect", "intersect_count", "intersect_pairs",
     "run_2set", "run_2set_c", "run_kset", "run_2set_bsr",
     "svs_generic", "run_svs", "validate_sorted",
     "ALGO_AUTO", "ALGO_MERGE", "ALGO_GALLOP", "ALGO_BITMAP", "VARIANT", "num_variants",
@@ -572,6 +572,36 @@ def intersect(set_a, set_b, out=None, *, algo: int = ALGO_AUTO,
     ctx.check(lib.setops_gpu_intersect(ctx.handle, a.ptr, a.n, b.ptr, b.n, optr, ocap,
                                        C.byref(n), flags))
     return out, int(n.value)
+
+
+def intersect_pairs(pairs, outs=None, *, algo: int = ALGO_AUTO,
+                    ctx: Context | None = None):
+    """A ∩ B for many independent pairs of host arrays in one call
+    (setops_gpu_intersect_pairs): returns [(out, length)], each what
+    intersect() gives for that pair.  `outs` are host uint32 arrays of
+    capacity >= min(|A|, |B|) (allocated when not given); pinned inputs and
+    outputs let search-band pairs be read in place while the other pairs'
+    inputs are copied."""
+    ctx = ctx or default_context()
+    bufs = [(_Buf(x), _Buf(y)) for x, y in pairs]
+    for a, b in bufs:
+        if a.device or b.device:
+            raise SetopsError(_lib.ERR_INVALID, "intersect_pairs takes host arrays")
+    n = len(bufs)
+    if outs is None:
+        outs = [np.empty(max(min(a.n, b.n), 1), np.uint32) for a, b in bufs]
+    for o in outs:
+        if not (isinstance(o, np.ndarray) and o.dtype == np.uint32 and o.flags.c_contiguous):
+            raise SetopsError(_lib.ERR_INVALID, "host output must be a contiguous uint32 array")
+    P = C.c_void_p * max(n, 1)
+    S = C.c_size_t * max(n, 1)
+    pa, pb = P(*[a.ptr for a, _ in bufs]), P(*[b.ptr for _, b in bufs])
+    la, lb = S(*[a.n for a, _ in bufs]), S(*[b.n for _, b in bufs])
+    po, co = P(*[o.ctypes.data for o in outs]), S(*[o.size for o in outs])
+    lens = S()
+    ctx.check(lib.setops_gpu_intersect_pairs(ctx.handle, n, pa, la, pb, lb, po, co, lens,
+                                             HOST | algo))
+    return [(outs[i], int(lens[i])) for i in range(n)]
 
 
 def _run_visitor(set_a, set_b, visitor, algo: int, ctx: Context | None) -> None:

@@ -79,6 +79,7 @@ SIGNATURES = [
     ("setops_gpu_intersect_count", C.c_int, [vp, vp, sz, vp, sz, u64p, uint]),
     ("setops_gpu_intersect", C.c_int, [vp, vp, sz, vp, sz, vp, sz, szp, uint]),
     ("setops_gpu_intersect_async", C.c_int, [vp, vp, sz, vp, sz, vp, sz, vp, uint]),
+    ("setops_gpu_intersect_pairs", C.c_int, [vp, sz, vp, vp, vp, vp, vp, vp, vp, uint]),
     ("setops_gpu_intersect_bsr_count", C.c_int, [vp, vp, vp, sz, vp, vp, sz, u64p, uint]),
     ("setops_gpu_intersect_bsr", C.c_int, [vp, vp, vp, sz, vp, vp, sz, vp, vp, sz, szp, uint]),
     ("setops_gpu_bsr_from_sorted", C.c_int, [vp, vp, sz, vp, vp, szp, uint]),

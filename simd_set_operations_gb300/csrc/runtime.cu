@@ -443,8 +443,13 @@ int setops_gpu_destroy(setops_ctx *ctx) {
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   for (DevBuf *b : ctx->all_bufs())
     if (b->p) cudaFree(b->p);
+  if (ctx->aux) cudaStreamSynchronize(ctx->aux);
   if (ctx->dsmall) cudaFree(ctx->dsmall);
   if (ctx->hres) cudaFreeHost(ctx->hres);
+  if (ctx->hlens) cudaFreeHost(ctx->hlens);
+  if (ctx->ev_main) cudaEventDestroy(ctx->ev_main);
+  if (ctx->ev_aux) cudaEventDestroy(ctx->ev_aux);
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->own) cudaStreamDestroy(ctx->own);
   delete ctx;
   return SETOPS_OK;
@@ -687,6 +692,195 @@ int setops_gpu_intersect_async(setops_ctx *ctx, const uint32_t *a, size_t na,
     return ctx_fail(ctx, SETOPS_ERR_INVALID, "async call with host pointers");
   return intersect_impl(ctx, a, na, b, nb, out, out_cap, nullptr, len_dev,
                         flags);
+}
+
+// ---- many pairs with host inputs ----
+//
+// One call for npairs independent pairs in host memory, results to host
+// memory, each result what setops_gpu_intersect gives for the pair.  A
+// search-band pair whose inputs and output are device-readable (pinned)
+// host memory is read in place (as in the one-pair call); here those pairs
+// run on a second stream while the other pairs' inputs are copied over the
+// host link, so the copies and the in-place searches overlap.  Kernels never
+// overlap each other: the copied pairs' kernels wait for the in-place ones
+// (two cooperative launches sharing the GPU could each wait for CTAs the
+// other holds).  All scratch is reserved before any work is queued, so no
+// buffer is reallocated while work is in flight.  Pairs with a pageable
+// output take the one-pair call afterwards.
+
+namespace {
+enum PairKind { kEmpty = 0, kInPlace = 1, kCopied = 2, kOnePairCall = 3 };
+constexpr int kCopySlots = 3;  // copied pairs whose inputs may be in flight at once
+}  // namespace
+
+int setops_gpu_intersect_pairs(setops_ctx *ctx, size_t npairs,
+                               const uint32_t *const *a, const size_t *na,
+                               const uint32_t *const *b, const size_t *nb,
+                               uint32_t *const *out, const size_t *out_cap,
+                               size_t *out_len, unsigned flags) {
+  if (!ctx) return SETOPS_ERR_INVALID;
+  if (npairs == 0) return SETOPS_OK;
+  if (!a || !na || !b || !nb || !out || !out_cap || !out_len)
+    return ctx_fail(ctx, SETOPS_ERR_INVALID, "NULL pair array");
+  if (!(flags & SETOPS_HOST))
+    return ctx_fail(ctx, SETOPS_ERR_INVALID,
+                    "setops_gpu_intersect_pairs takes host pointers (SETOPS_HOST)");
+  for (size_t i = 0; i < npairs; ++i) {
+    const uint64_t mn = std::min<uint64_t>(na[i], nb[i]);
+    if ((na[i] && !a[i]) || (nb[i] && !b[i]) || (mn && !out[i]))
+      return ctx_fail(ctx, SETOPS_ERR_INVALID, "pair " + std::to_string(i) + ": NULL pointer");
+    if (out_cap[i] < mn)
+      return ctx_fail(ctx, SETOPS_ERR_CAPACITY,
+                      "pair " + std::to_string(i) + ": out_cap " + std::to_string(out_cap[i]) +
+                          " < min(na, nb) " + std::to_string(mn));
+  }
+  CK(cudaSetDevice(ctx->device));
+
+  // ---- plan ----
+  struct Plan {
+    int kind = kEmpty;
+    Choice c;
+    const uint32_t *da = nullptr, *db = nullptr;
+    uint32_t *dout = nullptr;
+    int slot = 0;
+  };
+  std::vector<Plan> plan(npairs);
+  uint64_t max_mn = 1, max_status = 1;
+  uint64_t slot_a[kCopySlots] = {}, slot_b[kCopySlots] = {};
+  int n_in_place = 0, n_copied = 0;
+  for (size_t i = 0; i < npairs; ++i) {
+    Plan &q = plan[i];
+    const uint64_t mn = std::min<uint64_t>(na[i], nb[i]);
+    if (mn == 0) continue;
+    q.c = ctx_choose(ctx, na[i], nb[i], false, flags);
+    void *vo = device_view(out[i]);
+    void *va = device_view(a[i]), *vb = device_view(b[i]);
+    if (!vo) {
+      q.kind = kOnePairCall;
+      continue;
+    }
+    q.dout = static_cast<uint32_t *>(vo);
+    if (va && vb && read_in_place(q.c)) {
+      q.kind = kInPlace;
+      q.da = static_cast<const uint32_t *>(va);
+      q.db = static_cast<const uint32_t *>(vb);
+      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && q.c.variant == 0) q.c.variant = 3;
+      ++n_in_place;
+    } else {
+      q.kind = kCopied;
+      q.slot = n_copied % kCopySlots;
+      slot_a[q.slot] = std::max<uint64_t>(slot_a[q.slot], na[i]);
+      slot_b[q.slot] = std::max<uint64_t>(slot_b[q.slot], nb[i]);
+      ++n_copied;
+    }
+    max_mn = std::max(max_mn, mn);
+    // at least what any kernel's launch reserves: tiles of the pair plus
+    // per-CTA words for a full grid (at most 64 CTAs per SM)
+    max_status = std::max<uint64_t>(max_status,
+                                    (na[i] + nb[i]) / 1024 + 2 + 2 * 64 * uint64_t(ctx->sms));
+  }
+
+  // ---- scratch, before anything is queued ----
+  RK(buf_reserve(ctx, ctx->stage0, max_mn * 4));
+  RK(ctx_status_words(ctx, max_status));
+  RK(buf_reserve(ctx, ctx->plen, npairs * sizeof(uint64_t)));
+  for (int s = 0; s < kCopySlots; ++s) {
+    if (slot_a[s]) RK(buf_reserve(ctx, ctx->in[2 * s], slot_a[s] * 4));
+    if (slot_b[s]) RK(buf_reserve(ctx, ctx->in[2 * s + 1], slot_b[s] * 4));
+  }
+  if (ctx->hlens_cap < npairs) {
+    if (ctx->hlens) {
+      CK(cudaStreamSynchronize(ctx->st));
+      CK(cudaFreeHost(ctx->hlens));
+      ctx->hlens = nullptr;
+      ctx->hlens_cap = 0;
+    }
+    const size_t want = std::max<size_t>(npairs, 64);
+    CK(cudaMallocHost(&ctx->hlens, want * sizeof(uint64_t)));
+    ctx->hlens_cap = want;
+  }
+  if (!ctx->aux) {
+    CK(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_main, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_aux, cudaEventDisableTiming));
+  }
+  uint64_t *plen = static_cast<uint64_t *>(ctx->plen.p);
+  const cudaStream_t main_st = ctx->st;
+  auto job = [&](size_t i, const uint32_t *da, const uint32_t *db) {
+    PairJob j;
+    j.a = da;
+    j.b = db;
+    j.na = na[i];
+    j.nb = nb[i];
+    j.out = plan[i].dout;
+    j.out_cap = out_cap[i];
+    j.len_dev = plen + i;
+    j.choice = plan[i].c;
+    return j;
+  };
+
+  // ---- in-place pairs on the second stream (after the main stream's queued work) ----
+  int rc = SETOPS_OK;
+  CK(cudaEventRecord(ctx->ev_main, main_st));
+  CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_main, 0));
+  if (n_in_place) {
+    ctx->st = ctx->aux;  // launches, and their epoch clears, go to the second stream
+    for (size_t i = 0; i < npairs && rc == SETOPS_OK; ++i)
+      if (plan[i].kind == kInPlace) rc = ctx_launch_pair(ctx, job(i, plan[i].da, plan[i].db));
+    ctx->st = main_st;
+  }
+  if (rc == SETOPS_OK) {
+    const cudaError_t e = cudaEventRecord(ctx->ev_aux, ctx->aux);
+    if (e != cudaSuccess) rc = ctx_cuda(ctx, e, "cudaEventRecord");
+  }
+
+  // ---- copied pairs on the main stream: the first kCopySlots pairs' copies
+  // start at once; every kernel waits for the in-place pairs ----
+  std::vector<size_t> copied;
+  for (size_t i = 0; i < npairs; ++i)
+    if (plan[i].kind == kCopied) copied.push_back(i);
+  auto copy_in = [&](size_t i) -> int {
+    const int s = plan[i].slot;
+    CK(cudaMemcpyAsync(ctx->in[2 * s].p, a[i], na[i] * 4, cudaMemcpyHostToDevice, main_st));
+    CK(cudaMemcpyAsync(ctx->in[2 * s + 1].p, b[i], nb[i] * 4, cudaMemcpyHostToDevice, main_st));
+    return SETOPS_OK;
+  };
+  for (size_t k = 0; k < copied.size() && k < size_t(kCopySlots) && rc == SETOPS_OK; ++k)
+    rc = copy_in(copied[k]);
+  if (rc == SETOPS_OK) {
+    const cudaError_t e = cudaStreamWaitEvent(main_st, ctx->ev_aux, 0);
+    if (e != cudaSuccess) rc = ctx_cuda(ctx, e, "cudaStreamWaitEvent");
+  }
+  for (size_t k = 0; k < copied.size() && rc == SETOPS_OK; ++k) {
+    const size_t i = copied[k];
+    // a slot is refilled only after the kernel that read it (stream order)
+    if (k >= size_t(kCopySlots)) rc = copy_in(i);
+    if (rc != SETOPS_OK) break;
+    const int s = plan[i].slot;
+    rc = ctx_launch_pair(ctx, job(i, static_cast<const uint32_t *>(ctx->in[2 * s].p),
+                                  static_cast<const uint32_t *>(ctx->in[2 * s + 1].p)));
+  }
+  if (rc != SETOPS_OK) {
+    cudaStreamSynchronize(ctx->aux);
+    cudaStreamSynchronize(main_st);
+    return rc;
+  }
+
+  // ---- every length in one copy; the main stream has waited for the second ----
+  if (n_in_place + n_copied > 0)
+    CK(cudaMemcpyAsync(ctx->hlens, plen, npairs * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                       main_st));
+  RK(ctx_check_device(ctx));  // synchronises the main stream, reads the error word
+  for (size_t i = 0; i < npairs; ++i) {
+    if (plan[i].kind == kEmpty) out_len[i] = 0;
+    else if (plan[i].kind != kOnePairCall) out_len[i] = size_t(ctx->hlens[i]);
+  }
+  // pairs with a pageable output: one call each
+  for (size_t i = 0; i < npairs; ++i)
+    if (plan[i].kind == kOnePairCall)
+      RK(setops_gpu_intersect(ctx, a[i], na[i], b[i], nb[i], out[i], out_cap[i], &out_len[i],
+                              flags));
+  return SETOPS_OK;
 }
 
 // ---- 2-set BSR ----

@@ -71,6 +71,11 @@ struct setops_ctx {
   setops::DevBuf stage0, stage1;
   setops::DevBuf inter[2];
   setops::DevBuf units;  // batch: the long-pair unit map
+  setops::DevBuf plen;   // multi-pair host call: per-pair result lengths
+  cudaStream_t aux = nullptr;           // multi-pair host call: the in-place pairs' stream
+  cudaEvent_t ev_main = nullptr, ev_aux = nullptr;
+  uint64_t *hlens = nullptr;            // pinned host copy of plen
+  size_t hlens_cap = 0;                 // entries
   uint32_t epoch = 1;
   uint64_t launches = 0;
   std::map<const void *, int> occ;
@@ -80,7 +85,8 @@ struct setops_ctx {
 
   std::vector<setops::DevBuf *> all_bufs() {
     std::vector<setops::DevBuf *> v = {&status, &out0, &out1, &stage0,
-                                       &stage1, &inter[0], &inter[1], &units};
+                                       &stage1, &inter[0], &inter[1], &units,
+                                       &plen};
     for (auto &b : in) v.push_back(&b);
     return v;
   }

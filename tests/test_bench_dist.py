@@ -79,4 +79,4 @@ def test_touched_bytes_and_summary():
     assert bench.algorithmic_bytes(1 << 24, 1 << 24, 167_772) == 134_888_816
     s = bench.summarize({"frac": 0.4123}, None, None, None, None, None, None)
     assert s == {"headline_frac": 0.412, "sweep_e2e_pairs_per_s": None,
-                 "sweep_cpu_pairs_per_s": None}
+                 "sweep_e2e_per_call_pairs_per_s": None, "sweep_cpu_pairs_per_s": None}

@@ -269,6 +269,41 @@ def _pinned(x: np.ndarray) -> np.ndarray:
     return v  # (the view's base holds the pinned tensor)
 
 
+def test_intersect_pairs_host(ctx, orc):
+    """One setops_gpu_intersect_pairs call over mixed host pairs -- search-band
+    pairs with pinned inputs and outputs (read in place on the second stream),
+    balanced pairs (copied; more than three, so copy slots are reused), pairs
+    with pageable inputs or outputs, empty pairs, operands swapped -- gives
+    every pair exactly naive_merge; so does a second call on the same context
+    with other sizes, and a call whose pairs are all of one kind."""
+    rng = np.random.default_rng(41)
+    shapes = [(1 << 10, 1 << 22, 10, "pp"), (200_000, 190_000, 2_000, "pp"),
+              (1 << 14, 1 << 22, 160, "pp"), (0, 1000, 0, "pp"), (70_000, 210_000, 700, "pp"),
+              (1 << 18, 1 << 22, 2_600, "pp"), (3000, 3000, 300, "ph"), (150_000, 150_000, 0, "pp"),
+              (1 << 12, 1 << 20, 40, "hp"), (5, 3, 1, "pp"), (1 << 20, 1 << 16, 600, "pp"),
+              (40_000, 45_000, 4_000, "pp")]
+    pairs, outs, wants = [], [], []
+    for na, nb, shared, kind in shapes:
+        a, b = pair_with_overlap(rng, na, nb, shared)
+        wants.append(orc.naive_merge(a, b))
+        pin_in, pin_out = kind[0] == "p", kind[1] == "p"
+        pairs.append((_pinned(a), _pinned(b)) if pin_in else (a, b))
+        cap = max(min(na, nb), 1)
+        outs.append(_pinned(np.zeros(cap, np.uint32)) if pin_out else np.zeros(cap, np.uint32))
+    for rep in range(2):
+        res = so.intersect_pairs(pairs, outs, ctx=ctx)
+        for i, ((got, n), want) in enumerate(zip(res, wants)):
+            assert n == want.size and np.array_equal(got[:n], want), (rep, i, shapes[i])
+        pairs = [(y, x) for x, y in pairs]  # swapped operands, same results
+    # only search-band pairs, then only balanced ones
+    for sel in ([0, 2, 5, 8], [1, 4, 7, 11]):
+        res = so.intersect_pairs([pairs[i] for i in sel], [outs[i] for i in sel], ctx=ctx)
+        for (got, n), i in zip(res, sel):
+            assert np.array_equal(got[:n], wants[i]), i
+    with pytest.raises(so.SetopsError):
+        so.intersect_pairs([pairs[1]], [np.zeros(1, np.uint32)], ctx=ctx)  # capacity
+
+
 def test_pinned_host_inputs_read_in_place(ctx, orc):
     """Host-pointer calls on pinned host memory: the kernels read the inputs
     in place (and write the result straight into a pinned output) where the
