@@ -1158,7 +1158,7 @@ def run_gb300(args):
     if not args.no_autotune:
         t0 = time.perf_counter()
         tab = so.autotune(band_lo=0, band_hi=16, max_elems=1 << 25, density=DENSITY, reps=3,
-                          ctx=ctx)
+                          bsr=False, ctx=ctx)
         policy = {"tuned_cells": tab["tuned_cells"], "seconds": time.perf_counter() - t0,
                   "device": tab["key"]["device"],
                   "table": {cell: so.describe_flags(f) for cell, f in tab["cells"].items()},

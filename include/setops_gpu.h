@@ -140,6 +140,13 @@ int setops_gpu_get_policy_class(const setops_ctx *ctx, int bsr, int ratio_band,
  * once per GPU and keep the table (setops_gpu_get_policy_class). */
 int setops_gpu_autotune(setops_ctx *ctx, int band_lo, int band_hi, size_t max_elems,
                         double density, int reps, int *tuned);
+/* The same for the BSR table: each cell's pair is generated as arrays (at
+ * most max_elems elements), encoded to BSR words on the device, and every
+ * BSR candidate (merge-family variants, among them the block-broadcast
+ * kernel, and search variants) is timed; all must give the same result
+ * words.  Bands and size classes are by word count, as the BSR choice is. */
+int setops_gpu_autotune_bsr(setops_ctx *ctx, int band_lo, int band_hi, size_t max_elems,
+                            double density, int reps, int *tuned);
 /* A text naming the GPU and driver (for keying a saved policy table). */
 int setops_gpu_device_key(setops_ctx *ctx, char *buf, size_t cap);
 

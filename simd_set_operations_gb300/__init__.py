@@ -399,27 +399,29 @@ SIZE_CLASSES = 4  # SETOPS_SIZE_CLASSES: smaller input < 2^12, < 2^16, < 2^22, l
 
 
 def autotune(*, band_lo: int = 0, band_hi: int = 16, max_elems: int = 1 << 25,
-             density: float = 0.05, reps: int = 3, cache: str | None = None,
+             density: float = 0.05, reps: int = 3, bsr: bool = True, cache: str | None = None,
              ctx: Context | None = None) -> dict:
-    """Fills the context's array policy table (algorithm and kernel variant
-    per size-ratio band and size class) by timing every candidate on
-    generated pairs (setops_gpu_autotune), and returns the table.  With
-    `cache` (a JSON file), a table saved there for the same GPU, driver and
-    tuning arguments is applied instead of tuning, and a new one is saved."""
+    """Fills the context's policy tables (algorithm and kernel variant per
+    size-ratio band and size class) by timing every candidate on generated
+    pairs -- the array table (setops_gpu_autotune) and, with `bsr`, the BSR
+    table (setops_gpu_autotune_bsr) -- and returns them.  With `cache` (a
+    JSON file), tables saved there for the same GPU, driver and tuning
+    arguments are applied instead of tuning, and new ones are saved."""
     import json
     import os
     ctx = ctx or default_context()
     key = {"device": ctx.device_key(), "band_lo": band_lo, "band_hi": band_hi,
-           "max_elems": int(max_elems), "density": float(density)}
+           "max_elems": int(max_elems), "density": float(density), "bsr": bool(bsr)}
     if cache and os.path.exists(cache):
         try:
             saved = json.load(open(cache))
         except (OSError, ValueError):
             saved = None
         if saved and saved.get("key") == key:
-            for cell, flags in saved["cells"].items():
-                band, cls = (int(x) for x in cell.split(","))
-                ctx.set_policy_class(False, band, cls, int(flags))
+            for name, is_bsr in (("cells", False), ("bsr_cells", True)):
+                for cell, flags in saved.get(name, {}).items():
+                    band, cls = (int(x) for x in cell.split(","))
+                    ctx.set_policy_class(is_bsr, band, cls, int(flags))
             return dict(saved, from_cache=True)
     n = C.c_int()
     ctx.check(lib.setops_gpu_autotune(ctx.handle, band_lo, band_hi, int(max_elems),
@@ -427,6 +429,13 @@ def autotune(*, band_lo: int = 0, band_hi: int = 16, max_elems: int = 1 << 25,
     cells = {f"{b},{c}": ctx.get_policy_class(False, b, c)
              for b in range(band_lo, band_hi + 1) for c in range(SIZE_CLASSES)}
     table = {"key": key, "tuned_cells": int(n.value), "cells": cells, "from_cache": False}
+    if bsr:
+        nb = C.c_int()
+        ctx.check(lib.setops_gpu_autotune_bsr(ctx.handle, band_lo, band_hi, int(max_elems),
+                                              float(density), reps, C.byref(nb)))
+        table["bsr_tuned_cells"] = int(nb.value)
+        table["bsr_cells"] = {f"{b},{c}": ctx.get_policy_class(True, b, c)
+                              for b in range(band_lo, band_hi + 1) for c in range(SIZE_CLASSES)}
     if cache:
         with open(cache, "w") as f:
             json.dump(table, f, indent=1)

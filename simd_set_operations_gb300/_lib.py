@@ -75,6 +75,8 @@ SIGNATURES = [
     ("setops_gpu_get_policy_class", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.POINTER(uint)]),
     ("setops_gpu_autotune", C.c_int, [vp, C.c_int, C.c_int, sz, C.c_double, C.c_int,
                                       C.POINTER(C.c_int)]),
+    ("setops_gpu_autotune_bsr", C.c_int, [vp, C.c_int, C.c_int, sz, C.c_double, C.c_int,
+                                      C.POINTER(C.c_int)]),
     ("setops_gpu_device_key", C.c_int, [vp, C.c_char_p, sz]),
     ("setops_gpu_intersect_count", C.c_int, [vp, vp, sz, vp, sz, u64p, uint]),
     ("setops_gpu_intersect", C.c_int, [vp, vp, sz, vp, sz, vp, sz, szp, uint]),

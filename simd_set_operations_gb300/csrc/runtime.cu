@@ -242,8 +242,12 @@ void ctx_default_policy(setops_ctx *ctx) {
                             : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
     unsigned u = (b < 5) ? (SETOPS_ALGO_BITMAP | SETOPS_VARIANT(kCoarseBitmap)) : v;
     // BSR below 32: the block-broadcast kernel (0.042-0.045 ms against
-    // 0.09-0.16 ms for the merge-path kernels materialising 2^20-word pairs)
-    unsigned w = (b < 5) ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(kBcastBsr)) : v;
+    // 0.09-0.16 ms for the merge-path kernels materialising 2^20-word pairs);
+    // above, the BSR search variants that exist: sampled thread per element,
+    // then a warp per element from 8192
+    unsigned w = (b < 5)    ? (SETOPS_ALGO_MERGE | SETOPS_VARIANT(kBcastBsr))
+                 : (b < 13) ? (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(0))
+                            : (SETOPS_ALGO_GALLOP | SETOPS_VARIANT(2));
     for (int c = 0; c < kSizeClasses; ++c) {
       ctx->policy[0][b][c] = u;
       ctx->policy[1][b][c] = w;
