@@ -118,11 +118,14 @@ const KernelInfo kBitmapU32[][2] = {
     {mk_window<128, 4, 5, 2048, 8, false, true>("window_128_a4_b5_t2048_m8_coarse"),
      mk_window<128, 4, 5, 2048, 8, true, true>("window_128_a4_b5_t2048_m8_coarse")},
     // 7: variant 0 with coarse bitmaps for sparse tiles (size ratios 2-31)
-    {mk_window<128, 4, 5, 2048, 8, false>("window_128_a4_b5_t2048_m8"),
-     mk_awindow<128, 4, 5, 2048, 8, true>("awindow_128_a4_b5_t2048_m8")},
+    {mk_window<128, 4, 5, 2048, 7, false>("window_128_a4_b5_t2048_m7"),
+     mk_awindow<128, 4, 5, 2048, 7, true>("awindow_128_a4_b5_t2048_m7")},
     // 8: materialise with both inputs copied ahead into shared memory
     // (cp.async; 0.045 vs 0.048 ms on the 2^24 pair); count mode keeps
-    // variant 0's kernel, which is faster there (0.035 vs 0.037 ms)
+    // variant 0's kernel, which is faster there (0.035 vs 0.037 ms).  Both
+    // with a launch bound of 7 CTAs per SM (the shared memory still allows
+    // 8): the code generated without the 64-register cap ran 0.0434 against
+    // 0.0443-0.0446 ms materialising and 0.0339 against 0.0350 counting
 };
 
 // GS lanes per element (1 = thread per element with IT interleaved
