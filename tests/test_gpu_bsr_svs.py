@@ -176,6 +176,32 @@ def test_svs_fused_shapes(ctx, orc, k, dens):
     assert want.size >= int(0.1 * min(s.size for s in sets))
 
 
+def test_kset_kernel_shapes(ctx, orc):
+    """The fused k-set kernel, count and materialise, equals svs_generic: the
+    k-set configuration's shape, sparse and dense tiles, the most sets (16),
+    identical sets, a set holding only a few far values, and tile edges
+    (smallest sets of 4095-4097 elements, its 4096-element tiles)."""
+    from simd_set_operations_gb300 import _svs
+    flags = so.ALGO_AUTO
+    rng = np.random.default_rng(701)
+    x = np.arange(50_000, dtype=np.uint32) * 3
+    groups = [ds.gen_kset(800 + k, 0.2, 0.05, 1 << 21, 1.0, k) for k in (3, 5, 8)]
+    groups += [ds.gen_kset(810 + k, dens, 0.1, 1 << 17, 0.5, k)
+               for k, dens in ((3, 0.001), (6, 0.3), (16, 0.05), (4, 0.9))]
+    groups += [[x, x, x], [x, x[::2], x[::3], x[1::5]],
+               [x, np.array([0, 3, 149_997, 4_000_000_000], np.uint32), x[::7]]]
+    for n in (4095, 4096, 4097, 8191, 12_289):
+        base = rand_set(rng, n, 1 << 24)
+        groups.append([base, np.union1d(base[::2], rand_set(rng, n, 1 << 24)).astype(np.uint32),
+                       np.union1d(base[::3], rand_set(rng, 2 * n, 1 << 24)).astype(np.uint32)])
+    for sets in groups:
+        sets = sorted(sets, key=len)
+        want = orc.svs_generic(sets)
+        out, n = _svs(sets, algo=flags, ctx=ctx)
+        assert np.array_equal(np.asarray(out[:n]), want), [s.size for s in sets]
+        assert _svs(sets, count_only=True, algo=flags, ctx=ctx) == want.size
+
+
 def test_svs_async(ctx, orc):
     """setops_gpu_svs_async: the result (or the count) on the device, no
     synchronisation; the fused path and the step-wise path (a set over 16x
