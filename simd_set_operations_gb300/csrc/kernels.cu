@@ -138,6 +138,9 @@ const KernelInfo kGallopU32[][2] = {
     GALLOP_ROW(256, 1, 8, 2048, false),  // 4: sampled, 8 interleaved
     GALLOP_ROW(256, 32, 1, 2048, false), // 5: sampled, warp per element
     GALLOP_ROW(256, 8, 1, 2048, false),  // 6: sampled, 9-ary
+    GALLOP_ROW(256, 1, 1, 2048, false),  // 7: sampled, thread per element, 256-element tiles
+    GALLOP_ROW(256, 1, 2, 2048, false),  // 8: the same, 512-element tiles (a launch of
+                                         //    2^18 elements: 512 CTAs, not 256)
 };
 const KernelInfo kGallopBsr[][2] = {
     GALLOP_ROW(256, 1, 4, 2048, true),

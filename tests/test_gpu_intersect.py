@@ -228,6 +228,10 @@ def test_default_policy_bands(ctx, orc):
         assert got == (algo, var), (band, got)
     for band in (0, 4):
         assert algo_var(ctx.get_policy(True, band)) == (so.ALGO_MERGE, 3)
+    # ratios 32-511 with a smaller set of 2^16 to 2^22 elements: the sampled
+    # search with 512-element tiles (variant 8)
+    for band in (5, 8):
+        assert algo_var(ctx.get_policy_class(False, band, 2)) == (so.ALGO_GALLOP, 8)
     rng = np.random.default_rng(21)
     for ratio in (1, 2, 3, 5, 16, 31, 32, 600, 9000):
         na = 2000 if ratio < 600 else 200
