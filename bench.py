@@ -575,8 +575,9 @@ def batch_leg(ctx, stream, npairs: int) -> dict:
     doffs = td(offs, np.int64)
     out = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
     lens = torch.zeros(npairs, dtype=torch.int64, device="cuda")
-    # autotune the batch policy on a sample (device arrays)
-    nt = min(npairs, 10000)
+    # autotune the batch policy on the batch itself (device arrays; a 10,000-
+    # pair sample once chose a search ratio that was 20 % slower on the whole)
+    nt = npairs
     ctx.check(L.setops_gpu_batch_autotune(ctx.handle, pool.data_ptr(), pool.numel(),
                                           *[a.data_ptr() for a in arrs], nt, 3, 0))
     v, r = C.c_int(), C.c_uint32()

@@ -19,13 +19,7 @@
 //   * the search inside the block is either GS == 1: one thread per element,
 //     branchless binary search, ITEMS interleaved per thread for memory-level
 //     parallelism; or GS > 1: GS lanes per element probing GS points per
-//     round ((GS+1)-ary narrowing via warp ballot).  Without a sample, a GS
-//     group starts with one round around a guess of the element's index in
-//     L from its value (L's first and last values bound the range): its GS
-//     probes sit at geometrically growing distances either side of the guess,
-//     so a guess within a few thousand places leaves a bracket of that size
-//     and saves two or three (GS+1)-ary rounds; a wrong guess only leaves a
-//     wider bracket.
+//     round ((GS+1)-ary narrowing via warp ballot).
 // Matches are staged per CTA (block scan per pass, order preserved) in a
 // scratch region at the CTA's first element (a CTA cannot emit more matches
 // than elements it owns); one warp-parallel look-back per CTA gives its
@@ -175,10 +169,6 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
     }
   };
 
-  // the value range of L, for the groups' index guesses (no sample)
-  const uint32_t l_first = (NSAMP == 0 && GS > 1 && nl > 0) ? __ldg(L) : 0u;
-  const uint32_t l_last = (NSAMP == 0 && GS > 1 && nl > 0) ? __ldg(L + nl - 1) : 0u;
-
   uint64_t cnt = 0;      // count mode (BSR: elements)
   uint64_t cta_cnt = 0;  // materialise: matches staged so far
   for (uint64_t base = s0; base < s1; base += TILE) {
@@ -240,41 +230,6 @@ __global__ void __launch_bounds__(NT) gallop_kernel(const GallopArgs p) {
         bracket(x, lo, len);
         if (len > 0) {
           uint64_t hi = lo + len;
-          if constexpr (NSAMP == 0 && GS > 1) if (hi - lo > uint64_t(64 * GS)) {
-            // one round around the value-proportional guess; lane gl probes at
-            // est - BASE << SH*(m-gl-1) (gl < m) or est + (gl == m ? 0 : BASE << SH*(gl-m-1))
-            constexpr int M = GS / 2;
-            constexpr int SH = GS >= 32 ? 1 : GS >= 16 ? 2 : GS >= 8 ? 3 : GS >= 4 ? 6 : 12;
-            constexpr uint64_t BASE = GS >= 16 ? 16 : 64;
-            const uint64_t est = (x <= l_first || l_last <= l_first) ? lo
-                                 : (x >= l_last) ? hi - 1
-                                                 : lo + guess_scale(x - l_first, l_last - l_first,
-                                                                    hi - 1 - lo);
-            const int kk = gl - M;
-            uint64_t xp;
-            bool ok;
-            if (kk < 0) {
-              const uint64_t d = BASE << (SH * (-kk - 1));
-              ok = est >= lo + d;
-              xp = ok ? est - d : lo;
-            } else {
-              const uint64_t d = kk == 0 ? 0 : (BASE << (SH * (kk - 1)));
-              xp = est + d;
-              ok = xp < hi;
-            }
-            const bool below = ok && __ldg(L + xp) < x;  // lower_bound > xp
-            const bool above = ok && !below;            // lower_bound <= xp
-            uint64_t l2 = below ? xp + 1 : lo, h2 = above ? xp : hi;
-#pragma unroll
-            for (int o = 1; o < GS; o <<= 1) {
-              const uint64_t lo_o = __shfl_xor_sync(gmask, l2, o);
-              const uint64_t hi_o = __shfl_xor_sync(gmask, h2, o);
-              l2 = lo_o > l2 ? lo_o : l2;
-              h2 = hi_o < h2 ? hi_o : h2;
-            }
-            lo = l2;
-            hi = h2;
-          }
           while (hi - lo > uint64_t(GS)) {
             const uint64_t span = hi - lo;
             const uint64_t xp = lo + (uint64_t(gl + 1) * span) / (GS + 1);

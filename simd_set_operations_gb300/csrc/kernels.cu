@@ -168,6 +168,11 @@ const KernelInfo &kset_kernel(bool mat) {
   return k[mat ? 1 : 0];
 }
 
+bool gallop_thread_per_element(int variant) {
+  // kGallopU32 rows 0, 4, 7 and 8 are GS = 1
+  return variant == 0 || variant == 4 || variant == 7 || variant == 8;
+}
+
 int num_variants(Algo algo, bool bsr) {
   if (algo == ALGO_MERGE) return bsr ? count_of(kMergeBsr) : count_of(kMergeU32);
   if (algo == ALGO_BITMAP) return bsr ? 0 : count_of(kBitmapU32);

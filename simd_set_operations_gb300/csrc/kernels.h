@@ -34,6 +34,12 @@ constexpr int kCoarseBitmap = 7;
 // SETOPS_ALGO_BITMAP variant whose materialise kernel stages both inputs in
 // shared memory by asynchronous copies (the default for size ratios below 2)
 constexpr int kStagedWindow = 8;
+// SETOPS_ALGO_GALLOP variant with eight lanes per element and no sample (the
+// in-place search over host memory), and whether a u32 search variant puts
+// one thread on each element (its rounds of single probes wait on the link
+// when the larger set is host memory)
+constexpr int kGallopNineWay = 3;
+bool gallop_thread_per_element(int variant);
 // BSR SETOPS_ALGO_MERGE variant that compares 32-word blocks of the two sets
 // all against all, a warp per run of blocks (bcast.cuh)
 constexpr int kBcastBsr = 3;

@@ -621,11 +621,11 @@ static int intersect_impl(setops_ctx *ctx, const uint32_t *a, size_t na,
       da = static_cast<const uint32_t *>(va);
       db = static_cast<const uint32_t *>(vb);
       // a search over host memory waits on the link for every probe round:
-      // under the default policy the thread-per-element variant gives way to
+      // under the default policy the thread-per-element variants give way to
       // nine-way rounds with eight lanes per element (0.28 against 0.37 ms
       // for 2^18 against 2^24 in place)
-      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && choice.variant == 0)
-        choice.variant = 3;
+      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && gallop_thread_per_element(choice.variant))
+        choice.variant = kGallopNineWay;
     } else if (mn > 0) {
       RK(ctx_stage_in(ctx, 0, a, na, &da));
       RK(ctx_stage_in(ctx, 1, b, nb, &db));
@@ -772,7 +772,8 @@ int setops_gpu_intersect_pairs(setops_ctx *ctx, size_t npairs,
       q.kind = kInPlace;
       q.da = static_cast<const uint32_t *>(va);
       q.db = static_cast<const uint32_t *>(vb);
-      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && q.c.variant == 0) q.c.variant = 3;
+      if ((flags & SETOPS_ALGO_MASK) == SETOPS_ALGO_AUTO && gallop_thread_per_element(q.c.variant))
+        q.c.variant = kGallopNineWay;
       ++n_in_place;
     } else {
       q.kind = kCopied;
