@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
             f = getattr(L, name)
             f.restype = sz
             f.argtypes = [vp, vp, sz, vp, vp, sz, vp, vp, vp]
+        L.orc_broadcast_bsr.restype = sz
+        L.orc_broadcast_bsr.argtypes = [C.c_int, vp, vp, sz, vp, vp, sz, vp, vp, vp]
         L.orc_svs_generic.restype = sz
         L.orc_svs_generic.argtypes = [C.POINTER(vp), C.POINTER(sz), sz, vp, vp,
                                       C.POINTER(vp)]
@@ -201,6 +203,18 @@ def branchless_merge_bsr_count(ba, sa, bb, sb) -> int:
 
 def galloping_bsr(ba, sa, bb, sb):
     return _bsr2("orc_galloping_bsr", ba, sa, bb, sb)
+
+
+def broadcast_bsr(ba, sa, bb, sb, w: int = 8):
+    """broadcast_*_bsr (setops/src/intersect/broadcast.rs:163-357) with
+    blocks of w bases."""
+    ba, sa, bb, sb = map(_u32, (ba, sa, bb, sb))
+    cnt = C.c_uint64()
+    m = max(min(ba.size, bb.size), 1)
+    ob, os_ = np.empty(m, np.uint32), np.empty(m, np.uint32)
+    n = lib().orc_broadcast_bsr(int(w), _ptr(ba), _ptr(sa), ba.size, _ptr(bb), _ptr(sb), bb.size,
+                                ob.ctypes.data, os_.ctypes.data, C.byref(cnt))
+    return ob[:n].copy(), os_[:n].copy()
 
 
 def svs_generic(sets) -> np.ndarray:

@@ -183,6 +183,55 @@ size_t orc_branchless_merge_bsr(const uint32_t *ba, const uint32_t *sa,
   return w;
 }
 
+/* broadcast_*_bsr (setops/src/intersect/broadcast.rs:163-357): blocks of w
+ * bases of A and of B compared all against all (w broadcasts of B's bases);
+ * a lane of A's block whose base equals one of B's takes the OR of the ANDed
+ * states (at most one term is non-zero: bases are distinct); lanes with an
+ * equal base and a non-zero state are visited in lane order; then A's block
+ * advances when its last base is at most B's last, B's when B's last is at
+ * most A's.  The remainders (fewer than w words of either set) go through
+ * branchless_merge_bsr, as in the reference. */
+size_t orc_broadcast_bsr(int w, const uint32_t *ba, const uint32_t *sa, size_t na,
+                         const uint32_t *bb, const uint32_t *sb, size_t nb,
+                         uint32_t *out_bases, uint32_t *out_states,
+                         uint64_t *elem_count) {
+  if (w < 1) w = 1;
+  if (w > 16) w = 16;
+  const size_t W = (size_t)w;
+  const size_t st_a = (na / W) * W, st_b = (nb / W) * W;
+  size_t ia = 0, ib = 0, n = 0;
+  uint64_t c = 0;
+  while (ia < st_a && ib < st_b) {
+    for (size_t l = 0; l < W; ++l) {
+      const uint32_t base = ba[ia + l];
+      uint32_t state = 0;
+      int eq = 0;
+      for (size_t m = 0; m < W; ++m) {
+        const int e = base == bb[ib + m];
+        eq |= e;
+        state |= e ? (sa[ia + l] & sb[ib + m]) : 0u;
+      }
+      if (eq && state != 0) {
+        if (out_bases) {
+          out_bases[n] = base;
+          out_states[n] = state;
+        }
+        ++n;
+        c += (uint64_t)__builtin_popcount(state);
+      }
+    }
+    const uint32_t a_max = ba[ia + W - 1], b_max = bb[ib + W - 1];
+    ia += W * (a_max <= b_max);
+    ib += W * (b_max <= a_max);
+  }
+  uint64_t c2 = 0;
+  const size_t n2 = orc_branchless_merge_bsr(ba + ia, sa + ia, na - ia, bb + ib, sb + ib, nb - ib,
+                                             out_bases ? out_bases + n : NULL,
+                                             out_states ? out_states + n : NULL, &c2);
+  if (elem_count) *elem_count = c + c2;
+  return n + n2;
+}
+
 /* galloping_bsr (setops/src/intersect/galloping.rs:51-76): galloping on the
  * bases of `large`, AND of states on a base match. */
 size_t orc_galloping_bsr(const uint32_t *ba, const uint32_t *sa, size_t na,

@@ -86,6 +86,14 @@ size_t orc_galloping_bsr(const uint32_t *ba, const uint32_t *sa, size_t na,
                          uint32_t *out_bases, uint32_t *out_states,
                          uint64_t *elem_count);
 
+/* broadcast_{sse,avx2,avx512}_bsr: setops/src/intersect/broadcast.rs:163-357,
+ * blocks of w = 4, 8 or 16 bases (w <= 16); the same outputs as
+ * orc_branchless_merge_bsr. */
+size_t orc_broadcast_bsr(int w, const uint32_t *ba, const uint32_t *sa, size_t na,
+                         const uint32_t *bb, const uint32_t *sb, size_t nb,
+                         uint32_t *out_bases, uint32_t *out_states,
+                         uint64_t *elem_count);
+
 /* ---- k-set --------------------------------------------------------------- */
 
 /* svs_generic with naive_merge as the 2-set function:

@@ -120,6 +120,13 @@ def test_bsr_roundtrip_and_merge(orc, seed):
         assert orc.branchless_merge_bsr_count(ba, sa, bc, sc) == orc.naive_merge_count(a, c)
         gb, gs = orc.galloping_bsr(ba, sa, bc, sc)
         assert np.array_equal(gb, ob) and np.array_equal(gs, os_)
+        # broadcast_{sse,avx2,avx512}_bsr (broadcast.rs:163-357), the scheme of
+        # the GPU's block-broadcast kernel: the same words for every width
+        for w in (4, 8, 16):
+            for x, y in (((ba, sa), (bc, sc)), ((bc, sc), (ba, sa))):
+                bb_, bs_ = orc.broadcast_bsr(*x, *y, w=w)
+                mb, ms = orc.branchless_merge_bsr(*x, *y)
+                assert np.array_equal(bb_, mb) and np.array_equal(bs_, ms), (w, n)
 
 
 @pytest.mark.parametrize("seed", range(4))
